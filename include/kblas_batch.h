@@ -1,0 +1,281 @@
+/*
+ * kblas_batch.h -- batched Cholesky / triangular routines (uniform and
+ * variable size) for GB300 (sm_103a).
+ *
+ * The uniform-size routines keep the reference names, argument lists, storage
+ * conventions and return codes of include/kblas_batch.h in the reference
+ * (citations beside each group). Storage is column-major. "Strided" forms take
+ * one device buffer and a stride in elements between consecutive matrices;
+ * the other forms take a DEVICE array of device pointers (the reference's
+ * kernels dereference the array on the device, e.g.
+ * src/batch_triangular/Xpotrf_batch_kernels.cuh:96).
+ *
+ * Conventions shared by every routine:
+ *  - all work is queued on the handle's stream; nothing synchronises the host
+ *    and nothing allocates memory, so the calls can be captured in CUDA graphs
+ *    once the workspace is allocated;
+ *  - info arrays are device int[batchCount]; 0 = success, +j = the leading
+ *    minor of order j is not positive definite (LAPACK xPOTRF semantics, the
+ *    meaning documented at reference include/kblas_batch.h:1482);
+ *  - flag combinations the reference leaves unimplemented (Upper factor,
+ *    POTRS/POSV with side = Left) return KBLAS_NotImplemented like the
+ *    reference; TRSM/TRMM additionally implement Upper, Unit and Right, which
+ *    the reference only reaches through MAGMA.
+ */
+#ifndef KBLAS_GB300_BATCH_H
+#define KBLAS_GB300_BATCH_H
+
+#include "kblas_defs.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct KBlasHandle;
+typedef struct KBlasHandle *kblasHandle_t;
+
+/* ---------------------------------------------------------------------------
+ * Workspace queries (reference include/kblas_batch.h:485,773,786,1100,1113,
+ * 1380,1391,2077,2089,2772,2785). Each call raises the handle's requested
+ * workspace to what the routine needs; kblasAllocateWorkspace then allocates.
+ * The uniform routines of this library need no workspace, so these only
+ * record zero-byte requests; they are kept so KBLAS callers link unchanged.
+ * ------------------------------------------------------------------------- */
+void kblas_syrk_batch_wsquery(kblasHandle_t handle, const int m, int batchCount);
+void kblas_trsm_batch_wsquery(kblasHandle_t handle, char side, int m, int n, int batchCount);
+void kblas_trsm_batch_strided_wsquery(kblasHandle_t handle, char side, int m, int n, int batchCount);
+void kblas_trmm_batch_wsquery(kblasHandle_t handle, char side, int m, int n, int batchCount);
+void kblas_trmm_batch_strided_wsquery(kblasHandle_t handle, char side, int m, int n, int batchCount);
+void kblas_potrf_batch_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_potrf_batch_strided_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_potrs_batch_wsquery(kblasHandle_t handle, const int m, const int n, int batchCount);
+void kblas_potrs_batch_strided_wsquery(kblasHandle_t handle, const int m, const int n, int batchCount);
+void kblas_posv_batch_wsquery(kblasHandle_t handle, char side, const int m, const int n, int batchCount);
+void kblas_posv_batch_strided_wsquery(kblasHandle_t handle, char side, const int m, const int n, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * SYRK: B := alpha*op(A)*op(A)^T + beta*B on the lower triangle of B (m x m);
+ * op(A) is m x n (trans = 'N') or A is n x m (trans = 'T').
+ * reference include/kblas_batch.h:631-728 (uplo = 'U' -> KBLAS_NotImplemented,
+ * as reference src/batch_triangular/Xsyrk_batch_drivers.cuh:133-136).
+ * ------------------------------------------------------------------------- */
+int kblasSsyrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const float alpha, const float **A_array, int lda,
+                     const float beta, float **B_array, int ldb, int batchCount);
+int kblasDsyrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const double alpha, const double **A_array, int lda,
+                     const double beta, double **B_array, int ldb, int batchCount);
+int kblasSsyrk_batch_strided(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                             const float alpha, const float *A, int lda, long strideA,
+                             const float beta, float *B, int ldb, long strideB, int batchCount);
+int kblasDsyrk_batch_strided(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                             const double alpha, const double *A, int lda, long strideA,
+                             const double beta, double *B, int ldb, long strideB, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * TRSM: solve op(A)*X = alpha*B (side 'L', A m x m) or X*op(A) = alpha*B
+ * (side 'R', A n x n); B is m x n and is overwritten by X.
+ * reference include/kblas_batch.h:948-1053.
+ * ------------------------------------------------------------------------- */
+int kblasStrsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha,
+                     const float **A_array, int lda, float **B_array, int ldb, int batchCount);
+int kblasDtrsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha,
+                     const double **A_array, int lda, double **B_array, int ldb, int batchCount);
+int kblasStrsm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const float alpha,
+                             const float *A, int lda, long strideA,
+                             float *B, int ldb, long strideB, int batchCount);
+int kblasDtrsm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const double alpha,
+                             const double *A, int lda, long strideA,
+                             double *B, int ldb, long strideB, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * TRMM: B := alpha*op(A)*B (side 'L') or alpha*B*op(A) (side 'R').
+ * reference include/kblas_batch.h:1232-1335.
+ * ------------------------------------------------------------------------- */
+int kblasStrmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha,
+                     const float **A_array, int lda, float **B_array, int ldb, int batchCount);
+int kblasDtrmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha,
+                     const double **A_array, int lda, double **B_array, int ldb, int batchCount);
+int kblasStrmm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const float alpha,
+                             const float *A, int lda, long strideA,
+                             float *B, int ldb, long strideB, int batchCount);
+int kblasDtrmm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const double alpha,
+                             const double *A, int lda, long strideA,
+                             double *B, int ldb, long strideB, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * POTRF: A = L*L^T in place (lower triangle only; the strict upper triangle
+ * is neither read nor written). reference include/kblas_batch.h:1486-1566.
+ * ------------------------------------------------------------------------- */
+int kblasSpotrf_batch(kblasHandle_t handle, char uplo, const int n,
+                      float **A_array, int lda, int batchCount, int *info_array);
+int kblasDpotrf_batch(kblasHandle_t handle, char uplo, const int n,
+                      double **A_array, int lda, int batchCount, int *info_array);
+int kblasSpotrf_batch_strided(kblasHandle_t handle, char uplo, const int n,
+                              float *A, int lda, long strideA, int batchCount, int *info_array);
+int kblasDpotrf_batch_strided(kblasHandle_t handle, char uplo, const int n,
+                              double *A, int lda, long strideA, int batchCount, int *info_array);
+
+/* ---------------------------------------------------------------------------
+ * POTRS: solve X*A = B with A = L*L^T given by its factor L (side 'R',
+ * uplo 'L'); B is m x n (m right-hand sides stored as rows) and is
+ * overwritten by X. reference include/kblas_batch.h:2190-2278.
+ * ------------------------------------------------------------------------- */
+int kblasSpotrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const float **A_array, int lda, float **B_array, int ldb, int batchCount);
+int kblasDpotrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const double **A_array, int lda, double **B_array, int ldb, int batchCount);
+int kblasSpotrs_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                              const float *A, int lda, long strideA,
+                              float *B, int ldb, long strideB, int batchCount);
+int kblasDpotrs_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                              const double *A, int lda, long strideA,
+                              double *B, int ldb, long strideB, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * POSV: POTRF then POTRS, fused into one kernel per size class. On exit A
+ * holds L and B holds X; for a matrix with info > 0, B is left unchanged
+ * (LAPACK xPOSV). reference include/kblas_batch.h:2896-2988.
+ * ------------------------------------------------------------------------- */
+int kblasSposv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     float **A_array, int lda, float **B_array, int ldb,
+                     int batchCount, int *info_array);
+int kblasDposv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     double **A_array, int lda, double **B_array, int ldb,
+                     int batchCount, int *info_array);
+int kblasSposv_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                             float *A, int lda, long strideA, float *B, int ldb, long strideB,
+                             int batchCount, int *info_array);
+int kblasDposv_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                             double *A, int lda, long strideA, double *B, int ldb, long strideB,
+                             int batchCount, int *info_array);
+
+/* ===========================================================================
+ * Extensions with no reference counterpart.
+ * ========================================================================= */
+
+/* Mixed-precision POSV (semantics of LAPACK DSPOSV, batched). The factor is
+ * computed in FP32 after symmetric diagonal scaling; each system is refined
+ * in FP64 (residual b - A*x and the update of x) until its normwise backward
+ * error reaches sqrt(n)*eps64; a system whose refinement stalls, or whose
+ * FP32 factorization meets a non-positive or tiny pivot, is re-solved with
+ * the FP64 factorization. iter_array (device int[batchCount], may be NULL):
+ * >= 0 refinement steps taken (A is unchanged); < 0 the FP64 path was used
+ * (A holds L): -1 FP32 pivot test failed, -2 refinement stalled, -3 step cap.
+ * info_array as for POSV. Needs workspace: kblas_posv_batch_mixed_wsquery. */
+void kblas_posv_batch_mixed_wsquery(kblasHandle_t handle, char side, const int m, const int n,
+                                    int batchCount);
+int kblasDposv_batch_mixed_strided(kblasHandle_t handle, char side, char uplo,
+                                   const int m, const int n,
+                                   double *A, int lda, long strideA,
+                                   double *B, int ldb, long strideB,
+                                   int batchCount, int *info_array, int *iter_array);
+int kblasDposv_batch_mixed(kblasHandle_t handle, char side, char uplo,
+                           const int m, const int n,
+                           double **A_array, int lda, double **B_array, int ldb,
+                           int batchCount, int *info_array, int *iter_array);
+
+/* Variable-size POSV in one persistent launch. m, n, lda, ldb are DEVICE
+ * int[batchCount] (the non-uniform convention of reference
+ * include/kblas_batch.h:829-845); max_m / max_n bound them. Matrices are
+ * binned by size class on the device, then one persistent kernel pulls work
+ * items from a device queue, factorizes, solves and (for _mixed) refines each
+ * system while it is resident on chip. No host synchronisation: the sequence
+ * can be captured in a CUDA graph. Needs workspace: kblas_posv_vbatch_wsquery.
+ * A non-positive n or an out-of-range lda/ldb gives info = -(argument index). */
+void kblas_posv_vbatch_wsquery(kblasHandle_t handle, const int max_n, int batchCount);
+int kblasDposv_vbatch(kblasHandle_t handle, char side, char uplo,
+                      int *m, int *n, int max_m, int max_n,
+                      double **A_array, int *lda, double **B_array, int *ldb,
+                      int batchCount, int *info_array);
+int kblasDposv_vbatch_mixed(kblasHandle_t handle, char side, char uplo,
+                            int *m, int *n, int max_m, int max_n,
+                            double **A_array, int *lda, double **B_array, int *ldb,
+                            int batchCount, int *info_array, int *iter_array);
+
+/* Status word of the last persistent launch on this handle (read by the host
+ * after the stream completes): KBLAS_Success, or KBLAS_Error_Timeout if a
+ * bounded device-side wait ran out. Synchronises the handle's stream. */
+int kblasGetDeviceStatus(kblasHandle_t handle);
+
+#ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+/* C++ overloads, reference include/kblas_batch.h:1393-1453 and siblings. */
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda,
+                      long strideA, int batchCount, int *info_array);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
+                      long strideA, int batchCount, int *info_array);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const float **A_array, int lda, float **B_array, int ldb, int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const double **A_array, int lda, double **B_array, int ldb, int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const float *A, int lda, long strideA, float *B, int ldb, long strideB,
+                      int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const double *A, int lda, long strideA, double *B, int ldb, long strideB,
+                      int batchCount);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     float **A, int lda, float **B, int ldb, int batchCount, int *info_array);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     double **A, int lda, double **B, int ldb, int batchCount, int *info_array);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     float *A, int lda, long strideA, float *B, int ldb, long strideB,
+                     int batchCount, int *info_array);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     double *A, int lda, long strideA, double *B, int ldb, long strideB,
+                     int batchCount, int *info_array);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha, const float **A, int lda,
+                     float **B, int ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha, const double **A, int lda,
+                     double **B, int ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha, const float *A, int lda,
+                     long strideA, float *B, int ldb, long strideB, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha, const double *A, int lda,
+                     long strideA, double *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha, const float **A, int lda,
+                     float **B, int ldb, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha, const double **A, int lda,
+                     double **B, int ldb, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const float alpha, const float *A, int lda,
+                     long strideA, float *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const double alpha, const double *A, int lda,
+                     long strideA, double *B, int ldb, long strideB, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const float alpha, const float **A, int lda, const float beta, float **B,
+                     int ldb, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const double alpha, const double **A, int lda, const double beta, double **B,
+                     int ldb, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const float alpha, const float *A, int lda, long strideA, const float beta,
+                     float *B, int ldb, long strideB, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const double alpha, const double *A, int lda, long strideA,
+                     const double beta, double *B, int ldb, long strideB, int batchCount);
+#endif /* __cplusplus */
+
+#endif /* KBLAS_GB300_BATCH_H */

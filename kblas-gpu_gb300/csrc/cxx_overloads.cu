@@ -1,0 +1,130 @@
+// cxx_overloads.cu -- the C++ overload set of the batch API
+// (reference include/kblas_batch.h:493-576, 794-891, 1119-1177, 1396-1452,
+// 2094-2152, 2790-2855), forwarding to the C entry points.
+#include "kblas.h"
+
+int kblas_potrf_batch(kblasHandle_t h, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info) {
+  return kblasSpotrf_batch(h, uplo, n, A, lda, batchCount, info);
+}
+int kblas_potrf_batch(kblasHandle_t h, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info) {
+  return kblasDpotrf_batch(h, uplo, n, A, lda, batchCount, info);
+}
+int kblas_potrf_batch(kblasHandle_t h, char uplo, const int n, float *A, int lda, long strideA,
+                      int batchCount, int *info) {
+  return kblasSpotrf_batch_strided(h, uplo, n, A, lda, strideA, batchCount, info);
+}
+int kblas_potrf_batch(kblasHandle_t h, char uplo, const int n, double *A, int lda, long strideA,
+                      int batchCount, int *info) {
+  return kblasDpotrf_batch_strided(h, uplo, n, A, lda, strideA, batchCount, info);
+}
+
+int kblas_potrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const float **A, int lda, float **B, int ldb, int batchCount) {
+  return kblasSpotrs_batch(h, side, uplo, m, n, A, lda, B, ldb, batchCount);
+}
+int kblas_potrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const double **A, int lda, double **B, int ldb, int batchCount) {
+  return kblasDpotrs_batch(h, side, uplo, m, n, A, lda, B, ldb, batchCount);
+}
+int kblas_potrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const float *A, int lda, long strideA, float *B, int ldb, long strideB,
+                      int batchCount) {
+  return kblasSpotrs_batch_strided(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount);
+}
+int kblas_potrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const double *A, int lda, long strideA, double *B, int ldb, long strideB,
+                      int batchCount) {
+  return kblasDpotrs_batch_strided(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount);
+}
+
+int kblas_posv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, float **A,
+                     int lda, float **B, int ldb, int batchCount, int *info) {
+  return kblasSposv_batch(h, side, uplo, m, n, A, lda, B, ldb, batchCount, info);
+}
+int kblas_posv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, double **A,
+                     int lda, double **B, int ldb, int batchCount, int *info) {
+  return kblasDposv_batch(h, side, uplo, m, n, A, lda, B, ldb, batchCount, info);
+}
+int kblas_posv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, float *A,
+                     int lda, long strideA, float *B, int ldb, long strideB, int batchCount,
+                     int *info) {
+  return kblasSposv_batch_strided(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount,
+                                  info);
+}
+int kblas_posv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, double *A,
+                     int lda, long strideA, double *B, int ldb, long strideB, int batchCount,
+                     int *info) {
+  return kblasDposv_batch_strided(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount,
+                                  info);
+}
+
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float **A, int lda, float **B, int ldb,
+                     int batchCount) {
+  return kblasStrsm_batch(h, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb, batchCount);
+}
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double **A, int lda, double **B,
+                     int ldb, int batchCount) {
+  return kblasDtrsm_batch(h, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb, batchCount);
+}
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float *A, int lda, long strideA,
+                     float *B, int ldb, long strideB, int batchCount) {
+  return kblasStrsm_batch_strided(h, side, uplo, trans, diag, m, n, alpha, A, lda, strideA, B, ldb,
+                                  strideB, batchCount);
+}
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double *A, int lda, long strideA,
+                     double *B, int ldb, long strideB, int batchCount) {
+  return kblasDtrsm_batch_strided(h, side, uplo, trans, diag, m, n, alpha, A, lda, strideA, B, ldb,
+                                  strideB, batchCount);
+}
+
+int kblas_trmm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float **A, int lda, float **B, int ldb,
+                     int batchCount) {
+  return kblasStrmm_batch(h, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb, batchCount);
+}
+int kblas_trmm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double **A, int lda, double **B,
+                     int ldb, int batchCount) {
+  return kblasDtrmm_batch(h, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb, batchCount);
+}
+int kblas_trmm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float *A, int lda, long strideA,
+                     float *B, int ldb, long strideB, int batchCount) {
+  return kblasStrmm_batch_strided(h, side, uplo, trans, diag, m, n, alpha, A, lda, strideA, B, ldb,
+                                  strideB, batchCount);
+}
+int kblas_trmm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double *A, int lda, long strideA,
+                     double *B, int ldb, long strideB, int batchCount) {
+  return kblasDtrmm_batch_strided(h, side, uplo, trans, diag, m, n, alpha, A, lda, strideA, B, ldb,
+                                  strideB, batchCount);
+}
+
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const int n,
+                     const float alpha, const float **A, int lda, const float beta, float **B,
+                     int ldb, int batchCount) {
+  return kblasSsyrk_batch(h, uplo, trans, m, n, alpha, A, lda, beta, B, ldb, batchCount);
+}
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const int n,
+                     const double alpha, const double **A, int lda, const double beta, double **B,
+                     int ldb, int batchCount) {
+  return kblasDsyrk_batch(h, uplo, trans, m, n, alpha, A, lda, beta, B, ldb, batchCount);
+}
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const int n,
+                     const float alpha, const float *A, int lda, long strideA, const float beta,
+                     float *B, int ldb, long strideB, int batchCount) {
+  return kblasSsyrk_batch_strided(h, uplo, trans, m, n, alpha, A, lda, strideA, beta, B, ldb, strideB,
+                                  batchCount);
+}
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const int n,
+                     const double alpha, const double *A, int lda, long strideA,
+                     const double beta, double *B, int ldb, long strideB, int batchCount) {
+  return kblasDsyrk_batch_strided(h, uplo, trans, m, n, alpha, A, lda, strideA, beta, B, ldb, strideB,
+                                  batchCount);
+}

@@ -1,0 +1,239 @@
+// potrf_posv.cu -- batched POTRF / POTRS / POSV, single and double precision,
+// strided and pointer-array forms.
+//
+// Entry points replace reference src/batch_triangular/Xpotrf_batch.cu:86-160,
+// Xpotrs_batch.cu:87-165 and Xposv_batch.cu:92-178 (same names, arguments,
+// flag support and return codes). Unlike the reference (host recursion over
+// TRSM + SYRK + cuBLAS GEMM, 4 launches at n = 32 and one HBM pass per level),
+// every call is ONE kernel launch: the team kernel for n <= 32 and the panel
+// kernel above (see chol_kernels.cuh).
+#include <stdio.h>
+
+#include "chol_kernels.cuh"
+#include "kblas_internal.h"
+#include "launch_util.h"
+
+namespace kgb {
+
+// Team size (lanes per matrix) for the n <= 32 kernel.
+static inline int team_size_for(int n, bool dbl) {
+  if (n <= 4) return 2;
+  if (n <= 12) return 4;
+  if (n <= 24) return dbl ? 8 : 8;
+  return 8;
+}
+
+template <typename T, int G, int MODE, class AccA, class AccB>
+static int launch_team(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
+                       long long batch, int *info) {
+  constexpr int NT = 128;
+  constexpr int TPB = NT / G;
+  int rc = (MODE == MODE_POTRF) ? 0 : (m < 8 ? m : 8);
+  size_t smem = (size_t)TPB * team_smem_elems<T>(n, rc) * sizeof(T);
+  auto kern = chol_team_kernel<T, G, NT, MODE, AccA, AccB>;
+  int st = set_smem(kern, smem);
+  if (st != KBLAS_Success) return st;
+  long long grid = (batch + TPB - 1) / TPB;
+  kern<<<(unsigned)grid, NT, smem, h->stream>>>(n, m, rc, A, lda, B, ldb, batch, info);
+  KGB_LAUNCH_CHECK("chol_team_kernel");
+  return KBLAS_Success;
+}
+
+template <typename T, int NB, int MODE, class AccA, class AccB>
+static int launch_blocked_nb(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
+                             long long batch, int *info, size_t smem, int rc) {
+  constexpr int KC = 32;
+  constexpr int NT = 256;
+  auto kern = chol_blocked_kernel<T, NB, KC, NT, MODE, AccA, AccB>;
+  int st = set_smem(kern, smem);
+  if (st != KBLAS_Success) return st;
+  kern<<<(unsigned)batch, NT, smem, h->stream>>>(n, m, rc, A, lda, B, ldb, batch, info);
+  KGB_LAUNCH_CHECK("chol_blocked_kernel");
+  return KBLAS_Success;
+}
+
+template <typename T, int MODE, class AccA, class AccB>
+static int launch_chol(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
+                       long long batch, int *info) {
+  if (n <= 32) {
+    switch (team_size_for(n, sizeof(T) == 8)) {
+      case 2: return launch_team<T, 2, MODE>(h, n, m, A, lda, B, ldb, batch, info);
+      case 4: return launch_team<T, 4, MODE>(h, n, m, A, lda, B, ldb, batch, info);
+      default: return launch_team<T, 8, MODE>(h, n, m, A, lda, B, ldb, batch, info);
+    }
+  }
+  const int limit = max_smem(h);
+  int rc = (MODE == MODE_POTRF) ? 0 : (m < 8 ? m : 8);
+  size_t s32 = blocked_smem_elems<T, 32, 32>(n, rc) * sizeof(T);
+  if ((long long)s32 <= limit)
+    return launch_blocked_nb<T, 32, MODE>(h, n, m, A, lda, B, ldb, batch, info, s32, rc);
+  if (rc > 1) rc = 1;
+  size_t s16 = blocked_smem_elems<T, 16, 32>(n, rc) * sizeof(T);
+  if ((long long)s16 <= limit)
+    return launch_blocked_nb<T, 16, MODE>(h, n, m, A, lda, B, ldb, batch, info, s16, rc);
+  fprintf(stderr, "KBLAS: batched Cholesky of order %d exceeds the on-chip panel limit\n", n);
+  return KBLAS_NotSupported;
+}
+
+// ------------------------------- checks ---------------------------------
+static inline int check_potrf(KBlasHandle *h, char uplo, int n, const void *A, int lda,
+                              int batch) {
+  if (!h) return KBLAS_Error_NotInitialized;
+  if (is_upper(uplo)) {
+    printf("Upper POTRF_BATCH is not implemented yet\n");
+    return KBLAS_NotImplemented;
+  }
+  if (!is_lower(uplo)) return KBLAS_Error_WrongInput;
+  if (n < 0 || batch < 0 || lda < (n > 1 ? n : 1)) return KBLAS_Error_WrongInput;
+  if (n > 0 && batch > 0 && !A) return KBLAS_Error_WrongInput;
+  return KBLAS_Success;
+}
+
+static inline int check_potrs(KBlasHandle *h, char side, char uplo, int m, int n, const void *A,
+                              int lda, const void *B, int ldb, int batch, const char *name) {
+  if (!h) return KBLAS_Error_NotInitialized;
+  if (is_left(side) || is_upper(uplo)) {
+    printf("(Left | Upper) %s_BATCH is not implemented yet\n", name);
+    return KBLAS_NotImplemented;
+  }
+  if (!is_right(side) || !is_lower(uplo)) return KBLAS_Error_WrongInput;
+  if (m < 0 || n < 0 || batch < 0 || lda < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1))
+    return KBLAS_Error_WrongInput;
+  if (n > 0 && batch > 0 && (!A || (m > 0 && !B))) return KBLAS_Error_WrongInput;
+  return KBLAS_Success;
+}
+
+template <typename T>
+static int potrf_strided(KBlasHandle *h, char uplo, int n, T *A, int lda, long long sA, int batch,
+                         int *info) {
+  int st = check_potrf(h, uplo, n, A, lda, batch);
+  if (st != KBLAS_Success) return st;
+  if (batch > 1 && sA < (long long)lda * n) return KBLAS_Error_WrongInput;
+  if (batch == 0) return KBLAS_Success;
+  if (n == 0) return zero_info(h, info, batch);
+  return launch_chol<T, MODE_POTRF>(h, n, 0, Strided<T>{A, sA}, lda, Strided<T>{nullptr, 0}, 1,
+                                    batch, info);
+}
+
+template <typename T>
+static int potrf_array(KBlasHandle *h, char uplo, int n, T **A, int lda, int batch, int *info) {
+  int st = check_potrf(h, uplo, n, A, lda, batch);
+  if (st != KBLAS_Success) return st;
+  if (batch == 0) return KBLAS_Success;
+  if (n == 0) return zero_info(h, info, batch);
+  return launch_chol<T, MODE_POTRF>(h, n, 0, PtrArr<T>{A}, lda, PtrArr<T>{nullptr}, 1, batch, info);
+}
+
+template <typename T>
+static int potrs_strided(KBlasHandle *h, char side, char uplo, int m, int n, const T *A, int lda,
+                         long long sA, T *B, int ldb, long long sB, int batch) {
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POTRS");
+  if (st != KBLAS_Success) return st;
+  if (batch > 1 && sB < (long long)ldb * n) return KBLAS_Error_WrongInput;
+  if (batch == 0 || n == 0 || m == 0) return KBLAS_Success;
+  return launch_chol<T, MODE_POTRS>(h, n, m, Strided<T>{const_cast<T *>(A), sA}, lda,
+                                    Strided<T>{B, sB}, ldb, batch, nullptr);
+}
+
+template <typename T>
+static int potrs_array(KBlasHandle *h, char side, char uplo, int m, int n, const T **A, int lda,
+                       T **B, int ldb, int batch) {
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POTRS");
+  if (st != KBLAS_Success) return st;
+  if (batch == 0 || n == 0 || m == 0) return KBLAS_Success;
+  return launch_chol<T, MODE_POTRS>(h, n, m, PtrArr<T>{const_cast<T **>(A)}, lda, PtrArr<T>{B},
+                                    ldb, batch, nullptr);
+}
+
+template <typename T>
+static int posv_strided(KBlasHandle *h, char side, char uplo, int m, int n, T *A, int lda,
+                        long long sA, T *B, int ldb, long long sB, int batch, int *info) {
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POSV");
+  if (st != KBLAS_Success) return st;
+  if (batch > 1 && (sA < (long long)lda * n || (m > 0 && sB < (long long)ldb * n)))
+    return KBLAS_Error_WrongInput;
+  if (batch == 0) return KBLAS_Success;
+  if (n == 0) return zero_info(h, info, batch);
+  if (m == 0)
+    return launch_chol<T, MODE_POTRF>(h, n, 0, Strided<T>{A, sA}, lda, Strided<T>{nullptr, 0}, 1,
+                                      batch, info);
+  return launch_chol<T, MODE_POSV>(h, n, m, Strided<T>{A, sA}, lda, Strided<T>{B, sB}, ldb, batch,
+                                   info);
+}
+
+template <typename T>
+static int posv_array(KBlasHandle *h, char side, char uplo, int m, int n, T **A, int lda, T **B,
+                      int ldb, int batch, int *info) {
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POSV");
+  if (st != KBLAS_Success) return st;
+  if (batch == 0) return KBLAS_Success;
+  if (n == 0) return zero_info(h, info, batch);
+  if (m == 0)
+    return launch_chol<T, MODE_POTRF>(h, n, 0, PtrArr<T>{A}, lda, PtrArr<T>{nullptr}, 1, batch, info);
+  return launch_chol<T, MODE_POSV>(h, n, m, PtrArr<T>{A}, lda, PtrArr<T>{B}, ldb, batch, info);
+}
+
+}  // namespace kgb
+
+using namespace kgb;
+
+extern "C" {
+
+int kblasSpotrf_batch(kblasHandle_t h, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info) {
+  return potrf_array<float>(h, uplo, n, A, lda, batchCount, info);
+}
+int kblasDpotrf_batch(kblasHandle_t h, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info) {
+  return potrf_array<double>(h, uplo, n, A, lda, batchCount, info);
+}
+int kblasSpotrf_batch_strided(kblasHandle_t h, char uplo, const int n, float *A, int lda,
+                              long strideA, int batchCount, int *info) {
+  return potrf_strided<float>(h, uplo, n, A, lda, strideA, batchCount, info);
+}
+int kblasDpotrf_batch_strided(kblasHandle_t h, char uplo, const int n, double *A, int lda,
+                              long strideA, int batchCount, int *info) {
+  return potrf_strided<double>(h, uplo, n, A, lda, strideA, batchCount, info);
+}
+
+int kblasSpotrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const float **A, int lda, float **B, int ldb, int batchCount) {
+  return potrs_array<float>(h, side, uplo, m, n, A, lda, B, ldb, batchCount);
+}
+int kblasDpotrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                      const double **A, int lda, double **B, int ldb, int batchCount) {
+  return potrs_array<double>(h, side, uplo, m, n, A, lda, B, ldb, batchCount);
+}
+int kblasSpotrs_batch_strided(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                              const float *A, int lda, long strideA, float *B, int ldb,
+                              long strideB, int batchCount) {
+  return potrs_strided<float>(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount);
+}
+int kblasDpotrs_batch_strided(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                              const double *A, int lda, long strideA, double *B, int ldb,
+                              long strideB, int batchCount) {
+  return potrs_strided<double>(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount);
+}
+
+int kblasSposv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, float **A,
+                     int lda, float **B, int ldb, int batchCount, int *info) {
+  return posv_array<float>(h, side, uplo, m, n, A, lda, B, ldb, batchCount, info);
+}
+int kblasDposv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n, double **A,
+                     int lda, double **B, int ldb, int batchCount, int *info) {
+  return posv_array<double>(h, side, uplo, m, n, A, lda, B, ldb, batchCount, info);
+}
+int kblasSposv_batch_strided(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                             float *A, int lda, long strideA, float *B, int ldb, long strideB,
+                             int batchCount, int *info) {
+  return posv_strided<float>(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount,
+                             info);
+}
+int kblasDposv_batch_strided(kblasHandle_t h, char side, char uplo, const int m, const int n,
+                             double *A, int lda, long strideA, double *B, int ldb, long strideB,
+                             int batchCount, int *info) {
+  return posv_strided<double>(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount,
+                              info);
+}
+
+}  // extern "C"

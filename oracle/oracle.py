@@ -1,0 +1,214 @@
+"""CPU oracle for the batched Cholesky / triangular path -- TEST INFRASTRUCTURE.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` may import this module: it is the checker and the timed CPU
+baseline, never part of the product path.
+
+It wraps ``liboracle.so`` (built from ``kblas_oracle.c`` / ``oracle_impl.h``,
+a C restatement of the LAPACK/BLAS routines the reference tests check
+against) with numpy-friendly helpers, plus the seeded input generators used
+by tests and the benchmark.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with gcc -O2 -fopenmp (portable flags only)."""
+    srcs = [os.path.join(_HERE, "kblas_oracle.c"), os.path.join(_HERE, "oracle_impl.h")]
+    if not force and os.path.exists(LIB_PATH):
+        t = os.path.getmtime(LIB_PATH)
+        if all(os.path.getmtime(s) <= t for s in srcs):
+            return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", tmp,
+           os.path.join(_HERE, "kblas_oracle.c"), "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(LIB_PATH)
+            P = C.c_void_p
+            I, Lg, D, F, Ch = C.c_int, C.c_long, C.c_double, C.c_float, C.c_char
+            for pfx, R in (("d", D), ("s", F)):
+                getattr(L, f"oracle_{pfx}potrf").argtypes = [I, P, I]
+                getattr(L, f"oracle_{pfx}potrf").restype = I
+                getattr(L, f"oracle_{pfx}potrs").argtypes = [I, I, P, I, P, I]
+                getattr(L, f"oracle_{pfx}posv").argtypes = [I, I, P, I, P, I]
+                getattr(L, f"oracle_{pfx}posv").restype = I
+                getattr(L, f"oracle_{pfx}trsm").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, P, I]
+                getattr(L, f"oracle_{pfx}trmm").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, P, I]
+                getattr(L, f"oracle_{pfx}syrk").argtypes = [Ch, Ch, I, I, R, P, I, R, P, I]
+                getattr(L, f"oracle_{pfx}potrf_batch").argtypes = [I, P, I, Lg, I, P, I]
+                getattr(L, f"oracle_{pfx}potrs_batch").argtypes = [I, I, P, I, Lg, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}posv_batch").argtypes = [I, I, P, I, Lg, P, I, Lg, I, P, I]
+                getattr(L, f"oracle_{pfx}trsm_batch").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, Lg, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}trmm_batch").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, Lg, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}syrk_batch").argtypes = [Ch, Ch, I, I, R, P, I, Lg, R, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}posv_vbatch").argtypes = [P, P, P, P, P, P, I, P, I]
+            L.oracle_backward_error_r.argtypes = [I, I, P, I, P, I, P, I]
+            L.oracle_backward_error_r.restype = D
+            L.oracle_backward_error_r_batch.argtypes = [I, I, P, I, Lg, P, I, Lg, P, I, Lg, I, P, I]
+            L.oracle_backward_error_r_vbatch.argtypes = [P, P, P, P, P, P, P, P, I, P, I]
+            L.oracle_factor_backward_error.argtypes = [I, P, I, P, I]
+            L.oracle_factor_backward_error.restype = D
+            L.oracle_lower_rel_diff.argtypes = [I, P, I, P, I]
+            L.oracle_lower_rel_diff.restype = D
+            L.oracle_max_threads.restype = I
+            _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _pfx(a: np.ndarray) -> str:
+    if a.dtype == np.float64:
+        return "d"
+    if a.dtype == np.float32:
+        return "s"
+    raise TypeError(a.dtype)
+
+
+def _b(c: str) -> bytes:
+    return c.encode()
+
+
+def nthreads_default() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+# --------------------------------------------------------------------------
+# Batched storage convention used throughout tests/bench: a batch of
+# column-major matrices is a numpy array of shape (batch, ncols, ld) in C
+# order, i.e. element (i, j) of matrix b is arr[b, j, i]; strideA = ld*ncols.
+# --------------------------------------------------------------------------
+
+def potrf_batch(A: np.ndarray, n: int, nthreads: int | None = None):
+    """In-place lower Cholesky of A[b, :, :] (shape (batch, n, lda)); returns info."""
+    assert A.flags.c_contiguous
+    batch, ncol, lda = A.shape
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"oracle_{_pfx(A)}potrf_batch")(n, _p(A), lda, ncol * lda, batch, _p(info),
+                                                   nthreads or nthreads_default())
+    return info
+
+
+def potrs_batch(L: np.ndarray, B: np.ndarray, m: int, n: int, nthreads: int | None = None):
+    batch, ncol, lda = L.shape
+    _, ncolb, ldb = B.shape
+    getattr(lib(), f"oracle_{_pfx(L)}potrs_batch")(m, n, _p(L), lda, ncol * lda, _p(B), ldb,
+                                                   ncolb * ldb, batch, nthreads or nthreads_default())
+
+
+def posv_batch(A: np.ndarray, B: np.ndarray, m: int, n: int, nthreads: int | None = None):
+    batch, ncol, lda = A.shape
+    _, ncolb, ldb = B.shape
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"oracle_{_pfx(A)}posv_batch")(m, n, _p(A), lda, ncol * lda, _p(B), ldb,
+                                                  ncolb * ldb, batch, _p(info),
+                                                  nthreads or nthreads_default())
+    return info
+
+
+def trsm_batch(side, uplo, trans, diag, m, n, alpha, A, B, nthreads=None):
+    batch, ncol, lda = A.shape
+    _, ncolb, ldb = B.shape
+    getattr(lib(), f"oracle_{_pfx(A)}trsm_batch")(_b(side), _b(uplo), _b(trans), _b(diag), m, n,
+                                                  alpha, _p(A), lda, ncol * lda, _p(B), ldb,
+                                                  ncolb * ldb, batch, nthreads or nthreads_default())
+
+
+def trmm_batch(side, uplo, trans, diag, m, n, alpha, A, B, nthreads=None):
+    batch, ncol, lda = A.shape
+    _, ncolb, ldb = B.shape
+    getattr(lib(), f"oracle_{_pfx(A)}trmm_batch")(_b(side), _b(uplo), _b(trans), _b(diag), m, n,
+                                                  alpha, _p(A), lda, ncol * lda, _p(B), ldb,
+                                                  ncolb * ldb, batch, nthreads or nthreads_default())
+
+
+def syrk_batch(uplo, trans, m, k, alpha, A, beta, Cm, nthreads=None):
+    batch, ncol, lda = A.shape
+    _, ncolc, ldc = Cm.shape
+    getattr(lib(), f"oracle_{_pfx(A)}syrk_batch")(_b(uplo), _b(trans), m, k, alpha, _p(A), lda,
+                                                  ncol * lda, beta, _p(Cm), ldc, ncolc * ldc,
+                                                  batch, nthreads or nthreads_default())
+
+
+def backward_error_r(A: np.ndarray, X: np.ndarray, B: np.ndarray, m: int, n: int,
+                     nthreads: int | None = None) -> np.ndarray:
+    """Per-system normwise backward error of X*A = B (A symmetric, lower)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    batch, ncol, lda = A.shape
+    _, ncx, ldx = X.shape
+    _, ncb, ldb = B.shape
+    eta = np.zeros(batch, dtype=np.float64)
+    lib().oracle_backward_error_r_batch(m, n, _p(A), lda, ncol * lda, _p(X), ldx, ncx * ldx,
+                                        _p(B), ldb, ncb * ldb, batch, _p(eta),
+                                        nthreads or nthreads_default())
+    return eta
+
+
+def factor_backward_error(A2d: np.ndarray, L2d: np.ndarray, n: int) -> float:
+    """||A - L L^T||_max / ||A||_max; arguments are (n, ld) arrays in C order
+    holding one column-major matrix."""
+    A2d = np.ascontiguousarray(A2d, dtype=np.float64)
+    L2d = np.ascontiguousarray(L2d, dtype=np.float64)
+    return lib().oracle_factor_backward_error(n, _p(A2d), A2d.shape[1], _p(L2d), L2d.shape[1])
+
+
+def lower_rel_diff(L1: np.ndarray, L2: np.ndarray, n: int) -> float:
+    L1 = np.ascontiguousarray(L1, dtype=np.float64)
+    L2 = np.ascontiguousarray(L2, dtype=np.float64)
+    return lib().oracle_lower_rel_diff(n, _p(L1), L1.shape[1], _p(L2), L2.shape[1])
+
+
+def posv_vbatch(ms, ns, As, ldas, Bs, ldbs, nthreads=None):
+    """Variable-size POSV over lists of numpy arrays (each (ncol, ld) C order)."""
+    batch = len(ns)
+    m = np.asarray(ms, dtype=np.int32)
+    n = np.asarray(ns, dtype=np.int32)
+    lda = np.asarray(ldas, dtype=np.int32)
+    ldb = np.asarray(ldbs, dtype=np.int32)
+    pa = np.array([a.ctypes.data for a in As], dtype=np.uint64)
+    pb = np.array([b.ctypes.data for b in Bs], dtype=np.uint64)
+    info = np.zeros(batch, dtype=np.int32)
+    lib().oracle_dposv_vbatch(_p(m), _p(n), _p(pa), _p(lda), _p(pb), _p(ldb), batch, _p(info),
+                              nthreads or nthreads_default())
+    return info
+
+
+def backward_error_r_vbatch(ms, ns, As, ldas, Xs, ldxs, Bs, ldbs, nthreads=None):
+    batch = len(ns)
+    m = np.asarray(ms, dtype=np.int32)
+    n = np.asarray(ns, dtype=np.int32)
+    lda = np.asarray(ldas, dtype=np.int32)
+    ldx = np.asarray(ldxs, dtype=np.int32)
+    ldb = np.asarray(ldbs, dtype=np.int32)
+    pa = np.array([a.ctypes.data for a in As], dtype=np.uint64)
+    px = np.array([x.ctypes.data for x in Xs], dtype=np.uint64)
+    pb = np.array([b.ctypes.data for b in Bs], dtype=np.uint64)
+    eta = np.zeros(batch, dtype=np.float64)
+    lib().oracle_backward_error_r_vbatch(_p(m), _p(n), _p(pa), _p(lda), _p(px), _p(ldx), _p(pb),
+                                         _p(ldb), batch, _p(eta), nthreads or nthreads_default())
+    return eta

@@ -1,0 +1,112 @@
+"""Generate the LAPACK/BLAS golden fixtures that pin the CPU oracle.
+
+The reference's batch tests judge every routine against host LAPACK/BLAS
+looped over the batch (testing/batch_triangular/test_Xpotrf_batch.cpp:317-338,
+test_Xposv_batch.cpp:313-338, test_Xtrsm_batch.cpp:330-360,
+test_Xtrmm_batch.cpp:346-354, test_Xsyrk_batch.cpp:405-417) and ship no golden
+vectors of their own. This script records what LAPACK/BLAS (scipy's bundled
+OpenBLAS: dpotrf/spotrf, dpotrs, dtrsm/strsm, dtrmm/strmm, dsyrk/ssyrk)
+returns on small seeded inputs, including non-SPD matrices with a known
+failing leading minor, so tests/test_oracle.py can check the C oracle against
+it on any machine (scipy is not needed at test time).
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+from scipy.linalg import blas, lapack
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+
+
+def rng(seed, stream):
+    return np.random.Generator(np.random.Philox(key=seed, counter=[0, 0, 0, stream]))
+
+
+def spd(n, r):
+    g = r.standard_normal((n, n))
+    return g @ g.T + n * np.eye(n)
+
+
+def lowtri(n, r):
+    a = np.tril(r.standard_normal((n, n)) / np.sqrt(n), -1)
+    return a + np.diag(r.uniform(1.0, 2.0, n))
+
+
+def main():
+    out = {}
+    r = rng(2024, 0)
+    sizes = [1, 2, 3, 7, 8, 9, 15, 16, 17, 31, 32, 33, 47, 63, 64, 65, 97]
+    for dt, name in ((np.float64, "d"), (np.float32, "s")):
+        potrf, potrs = (lapack.dpotrf, lapack.dpotrs) if name == "d" else (lapack.spotrf, lapack.spotrs)
+        trsm, trmm, syrk = ((blas.dtrsm, blas.dtrmm, blas.dsyrk) if name == "d"
+                            else (blas.strsm, blas.strmm, blas.ssyrk))
+        for n in sizes:
+            a = spd(n, r).astype(dt)
+            c, info = potrf(a, lower=1, clean=1)
+            out[f"{name}potrf_n{n}_A"] = a
+            out[f"{name}potrf_n{n}_L"] = np.tril(c)
+            out[f"{name}potrf_n{n}_info"] = np.int32(info)
+            for m in (1, 4):
+                b = r.standard_normal((m, n)).astype(dt)  # rows = right-hand sides
+                x, info2 = potrs(c, b.T.copy(), lower=1)
+                out[f"{name}posv_n{n}_m{m}_B"] = b
+                out[f"{name}posv_n{n}_m{m}_X"] = x.T.copy()
+        # non-SPD with a known failing leading minor k (1-based)
+        for n, k in ((1, 1), (5, 3), (8, 8), (16, 1), (17, 9), (32, 20), (33, 33), (64, 40),
+                     (97, 77)):
+            a = spd(n, r)
+            # pivot k of the untouched matrix, then push it to -1
+            piv = a[k - 1, k - 1]
+            if k > 1:
+                l11 = np.linalg.cholesky(a[: k - 1, : k - 1])
+                w = np.linalg.solve(l11, a[: k - 1, k - 1])
+                piv = a[k - 1, k - 1] - w @ w
+            a[k - 1, k - 1] -= piv + 1.0
+            a = a.astype(dt)
+            c, info = potrf(a, lower=1, clean=0)
+            assert info == k, (n, k, info)
+            out[f"{name}nonspd_n{n}_A"] = a
+            out[f"{name}nonspd_n{n}_info"] = np.int32(info)
+        # TRSM / TRMM all flag combinations on small shapes
+        for (m, n) in ((5, 3), (16, 16), (33, 7), (40, 24), (3, 40)):
+            for side in "LR":
+                ka = m if side == "L" else n
+                for uplo in "LU":
+                    for trans in "NT":
+                        for diag in "NU":
+                            a = lowtri(ka, r)
+                            if uplo == "U":
+                                a = a.T.copy()
+                            b = r.standard_normal((m, n))
+                            alpha = 1.5
+                            kw = dict(side=int(side == "R"), lower=int(uplo == "L"),
+                                      trans_a=int(trans == "T"), diag=int(diag == "U"))
+                            xs = trsm(alpha, a.astype(dt), b.astype(dt), **kw)
+                            xm = trmm(alpha, a.astype(dt), b.astype(dt), **kw)
+                            key = f"{name}tr_{side}{uplo}{trans}{diag}_m{m}_n{n}"
+                            out[key + "_A"] = a.astype(dt)
+                            out[key + "_B"] = b.astype(dt)
+                            out[key + "_trsm"] = xs
+                            out[key + "_trmm"] = xm
+        # SYRK lower, both transposes
+        for (m, k) in ((1, 1), (5, 3), (16, 16), (33, 17), (48, 40), (70, 9)):
+            for trans in "NT":
+                a = r.standard_normal((m, k) if trans == "N" else (k, m))
+                c0 = spd(m, r)
+                res = syrk(-1.0, a.astype(dt), beta=1.0, c=c0.astype(dt),
+                           trans=int(trans == "T"), lower=1)
+                key = f"{name}syrk_{trans}_m{m}_k{k}"
+                out[key + "_A"] = a.astype(dt)
+                out[key + "_C"] = c0.astype(dt)
+                out[key + "_R"] = np.tril(res)
+    path = os.path.join(HERE, "lapack_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, len(out), "arrays", os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main()

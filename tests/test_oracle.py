@@ -1,0 +1,134 @@
+"""The C oracle against the LAPACK/BLAS golden vectors (CPU only).
+
+Pins the oracle before it is trusted as the checker of the GPU library: every
+routine is compared with what LAPACK/BLAS returned on the same inputs
+(tests/golden/lapack_golden.npz, made by tests/golden/make_golden.py), and
+info codes of non-SPD matrices must match exactly.
+"""
+import re
+
+import numpy as np
+import pytest
+
+from gpu_util import eps
+
+
+def colmajor(a2d: np.ndarray, dtype=None):
+    """One row-major numpy matrix -> (1, ncols, ld=rows) column-major batch."""
+    a = np.asarray(a2d, dtype=dtype)
+    return np.array(a.T, order="C", copy=True)[None]
+
+
+def keys(golden, pat):
+    rx = re.compile(pat)
+    return sorted({m.group(1) for k in golden.files for m in [rx.match(k)] if m})
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_potrf_posv_vs_lapack(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    ns = sorted(int(x) for x in keys(golden, rf"{pfx}potrf_n(\d+)_A"))
+    assert ns, "no golden cases"
+    for n in ns:
+        A = golden[f"{pfx}potrf_n{n}_A"]
+        Lref = golden[f"{pfx}potrf_n{n}_L"]
+        a = colmajor(A, dt)
+        info = orc.potrf_batch(a, n, nthreads=1)
+        assert info[0] == int(golden[f"{pfx}potrf_n{n}_info"]) == 0
+        L = np.tril(a[0].T)
+        rel = np.abs(L - Lref).max() / np.abs(Lref).max()
+        assert rel <= 10 * n * eps(dt), (n, rel)
+        for m in (1, 4):
+            B = golden[f"{pfx}posv_n{n}_m{m}_B"]
+            Xref = golden[f"{pfx}posv_n{n}_m{m}_X"]
+            a2 = colmajor(A, dt)
+            b2 = colmajor(B, dt)  # (1, n, m): m x n column-major, ld = m
+            info2 = orc.posv_batch(a2, b2, m, n, nthreads=1)
+            assert info2[0] == 0
+            X = b2[0].T
+            err = np.abs(X - Xref).max() / np.abs(Xref).max()
+            assert err <= 100 * n * eps(dt), (n, m, err)
+            if pfx == "d":
+                eta = orc.backward_error_r(colmajor(A), b2.astype(np.float64), colmajor(B), m, n)
+                assert eta[0] <= 10 * n * eps(dt), (n, m, eta)
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_nonspd_info_exact(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    ns = sorted(int(x) for x in keys(golden, rf"{pfx}nonspd_n(\d+)_A"))
+    assert ns
+    for n in ns:
+        a = colmajor(golden[f"{pfx}nonspd_n{n}_A"], dt)
+        info = orc.potrf_batch(a, n, nthreads=1)
+        assert info[0] == int(golden[f"{pfx}nonspd_n{n}_info"]), n
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_trsm_trmm_vs_blas(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    cases = keys(golden, rf"{pfx}tr_(\w+_m\d+_n\d+)_A")
+    assert len(cases) >= 16 * 5
+    for c in cases:
+        flags, ms, ns = c.split("_")
+        side, uplo, trans, diag = flags
+        m, n = int(ms[1:]), int(ns[1:])
+        A = golden[f"{pfx}tr_{c}_A"]
+        B = golden[f"{pfx}tr_{c}_B"]
+        ka = m if side == "L" else n
+        for op, key in ((orc.trsm_batch, "trsm"), (orc.trmm_batch, "trmm")):
+            a = colmajor(A, dt)
+            b = colmajor(B, dt)
+            op(side, uplo, trans, diag, m, n, 1.5, a, b, nthreads=1)
+            ref = golden[f"{pfx}tr_{c}_{key}"]
+            got = b[0].T
+            err = np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-30)
+            assert err <= 50 * ka * eps(dt), (key, c, err)
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_syrk_vs_blas(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    cases = keys(golden, rf"{pfx}syrk_(\w_m\d+_k\d+)_A")
+    assert cases
+    for c in cases:
+        trans, ms, ks = c.split("_")
+        m, k = int(ms[1:]), int(ks[1:])
+        a = colmajor(golden[f"{pfx}syrk_{c}_A"], dt)
+        cm = colmajor(golden[f"{pfx}syrk_{c}_C"], dt)
+        orc.syrk_batch("L", trans, m, k, -1.0, a, 1.0, cm, nthreads=1)
+        ref = golden[f"{pfx}syrk_{c}_R"]
+        got = np.tril(cm[0].T)
+        scale = np.abs(golden[f"{pfx}syrk_{c}_C"]).max() + k * np.abs(golden[f"{pfx}syrk_{c}_A"]).max() ** 2
+        assert np.abs(got - ref).max() <= 10 * k * eps(dt) * scale, c
+
+
+def test_backward_error_detects_wrong_solution(orc):
+    """A planted mistake in the solution must blow the backward error up."""
+    rng = np.random.default_rng(1)
+    n, m = 24, 2
+    g = rng.standard_normal((n, n))
+    A = g @ g.T + n * np.eye(n)
+    B = rng.standard_normal((m, n))
+    X = np.linalg.solve(A, B.T).T
+    a, x, b = colmajor(A), colmajor(X), colmajor(B)
+    good = orc.backward_error_r(a, x, b, m, n)[0]
+    assert good <= 10 * n * 2.0 ** -53
+    X2 = X.copy()
+    X2[1, 5] *= 1 + 1e-9
+    bad = orc.backward_error_r(a, colmajor(X2), b, m, n)[0]
+    assert bad > 100 * good and bad > 10 * n * 2.0 ** -53
+
+
+def test_oracle_threads_agree(orc):
+    """OpenMP batching gives the same bits as a single thread."""
+    rng = np.random.default_rng(2)
+    n, batch = 20, 64
+    g = rng.standard_normal((batch, n, n))
+    a = np.einsum("bij,bkj->bik", g, g) + n * np.eye(n)
+    a1 = np.ascontiguousarray(a)
+    a2 = a1.copy()
+    i1 = orc.potrf_batch(a1, n, nthreads=1)
+    i2 = orc.potrf_batch(a2, n, nthreads=4)
+    assert (i1 == 0).all() and (i2 == 0).all()
+    assert np.array_equal(a1, a2)
