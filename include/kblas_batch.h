@@ -201,6 +201,13 @@ int kblasDposv_vbatch_mixed(kblasHandle_t handle, char side, char uplo,
                             double **A_array, int *lda, double **B_array, int *ldb,
                             int batchCount, int *info_array, int *iter_array);
 
+/* Override the launch-shape table of the persistent POSV kernels (mixed != 0:
+ * the mixed-precision table, else the plain FP64 one): per size class, the
+ * largest order n of the class, the team size in threads (2..256, a power of
+ * two) and the systems per work item. Six entries each; NULL restores the
+ * table compiled into the library. Used by the committed autotuner. */
+int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi);
+
 /* Status word of the last persistent launch on this handle (read by the host
  * after the stream completes): KBLAS_Success, or KBLAS_Error_Timeout if a
  * bounded device-side wait ran out. Synchronises the handle's stream. */

@@ -88,6 +88,7 @@ _SIG = {
     "kblasDposv_batch_mixed": (I, [P, CH, CH, I, I, P, I, P, I, I, P, P]),
     "kblasDposv_vbatch": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P]),
     "kblasDposv_vbatch_mixed": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P, P]),
+    "kblasSetPosvTuning": (I, [I, P, P, P]),
 }
 for _x, _R in (("S", F), ("D", D)):
     _SIG.update({

@@ -1,0 +1,127 @@
+// posv_launch.h -- host-side planning of the persistent POSV launches:
+// launch shape per size class, shared-memory budget, grid, workspace layout.
+#pragma once
+
+#include <string.h>
+
+#include "kblas_internal.h"
+#include "launch_util.h"
+#include "posv_core.cuh"
+#include "tuning_table.h"
+
+namespace kgb {
+
+constexpr int PC_MAX_N = 1024;          // largest order the persistent kernels take
+constexpr size_t PC_SMEM_BUDGET = 200 * 1024;
+
+struct PosvPlan {
+  PosvCfg cfg;
+  int smem = 0;           // dynamic shared memory per CTA
+  int grid = 0;           // persistent CTAs
+  size_t slot_bytes = 0;  // global scratch per CTA
+};
+
+// Process-wide override of the tuning table (set by the autotuner through
+// kblasSetPosvTuning); zero entries mean "use the compiled table".
+struct TuneOverride {
+  int set[2] = {0, 0};
+  PosvCfg cfg[2];
+};
+TuneOverride &tune_override();
+
+static inline PosvCfg default_cfg(bool mixed) {
+  PosvCfg c;
+  const int mn[] = KGB_TUNE_MIXED_NMAX, mt[] = KGB_TUNE_MIXED_TS, ms[] = KGB_TUNE_MIXED_SPI;
+  const int pn[] = KGB_TUNE_PLAIN_NMAX, pt[] = KGB_TUNE_PLAIN_TS, ps[] = KGB_TUNE_PLAIN_SPI;
+  for (int k = 0; k < PC_NCLS; k++) {
+    c.nmax[k] = mixed ? mn[k] : pn[k];
+    c.ts[k] = mixed ? mt[k] : pt[k];
+    c.spi[k] = mixed ? ms[k] : ps[k];
+  }
+  c.nmax[PC_NCLS - 1] = PC_MAX_N;
+  return c;
+}
+
+static inline PosvCfg current_cfg(bool mixed) {
+  TuneOverride &o = tune_override();
+  return o.set[mixed ? 1 : 0] ? o.cfg[mixed ? 1 : 0] : default_cfg(mixed);
+}
+
+static inline bool cfg_valid(const PosvCfg &c) {
+  for (int k = 0; k < PC_NCLS; k++) {
+    const int ts = c.ts[k];
+    if (!(ts == 2 || ts == 4 || ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256))
+      return false;
+    if (c.spi[k] < 1 || c.spi[k] * ts > PC_NT || (ts >= 64 && c.spi[k] > 15)) return false;
+    if (k && c.nmax[k] <= c.nmax[k - 1]) return false;
+  }
+  return c.nmax[PC_NCLS - 1] >= PC_MAX_N;
+}
+
+template <bool MIXED>
+static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
+  pl.cfg = current_cfg(MIXED);
+  if (!cfg_valid(pl.cfg)) return KBLAS_WrongConfig;
+  const size_t budget = (size_t)(max_smem(h) < (int)PC_SMEM_BUDGET ? max_smem(h) : (int)PC_SMEM_BUDGET);
+  size_t smem = 0;
+  for (int c = 0; c < PC_NCLS; c++) {
+    const int nlo = c ? pl.cfg.nmax[c - 1] + 1 : 1;
+    const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
+    if (nhi < nlo) continue;
+    const int nteams = PC_NT / pl.cfg.ts[c];
+    size_t b = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], true);
+    if (b > budget) b = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], false);
+    if (b > budget) return KBLAS_NotSupported;
+    if (b > smem) smem = b;
+  }
+  pl.smem = (int)smem;
+  auto kern = posv_persistent_kernel<MIXED>;
+  int st = set_smem(kern, smem);
+  if (st != KBLAS_Success) return st;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  pl.grid = h->sm_count * per_sm;
+  pl.slot_bytes = posv_slot_bytes(pl.cfg, max_n);
+  return KBLAS_Success;
+}
+
+// Device workspace layout shared by the uniform mixed and the variable-size
+// routines (offsets in bytes from the start of the handle's device data).
+struct PosvWs {
+  size_t header = 0;   // int[64]: [0] queue, [1] item count
+  size_t cnt = 0;      // int[max_n + 1]   systems per order n
+  size_t off = 0;      // int[max_n + 1]   first slot of order n in perm
+  size_t ioff = 0;     // int[max_n + 1]   first item of order n
+  size_t cursor = 0;   // int[max_n + 1]
+  size_t perm = 0;     // int[batch]
+  size_t items = 0;    // int4[batch]
+  size_t scratch = 0;  // grid * slot_bytes
+  size_t total = 0;
+};
+
+static inline PosvWs posv_ws_layout(int max_n, long long batch, bool binned, const PosvPlan &pl) {
+  PosvWs w;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o += (bytes + 255) / 256 * 256;
+    return at;
+  };
+  w.header = take(64 * sizeof(int));
+  if (binned) {
+    const size_t nb = (size_t)(max_n + 1) * sizeof(int);
+    w.cnt = take(nb);
+    w.off = take(nb);
+    w.ioff = take(nb);
+    w.cursor = take(nb);
+    w.perm = take((size_t)batch * sizeof(int));
+    w.items = take((size_t)batch * sizeof(int4));
+  }
+  w.scratch = take((size_t)pl.grid * pl.slot_bytes);
+  w.total = o;
+  return w;
+}
+
+}  // namespace kgb

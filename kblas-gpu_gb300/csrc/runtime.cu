@@ -235,16 +235,20 @@ void kblas_posv_batch_strided_wsquery(kblasHandle_t, char, const int, const int,
 
 void kblas_posv_batch_mixed_wsquery(kblasHandle_t h, char side, const int m, const int n,
                                     int batchCount) {
+  (void)side;
+  (void)m;
   if (!h) return;
   KBlasWorkspaceState need;
-  need.d_data_bytes = kgb::mixed_posv_workspace_bytes(side, m, n, batchCount);
+  need.d_data_bytes = kgb::mixed_posv_ws_bytes(h, n, batchCount);
   h->ws.requested.pad(need);
 }
 
 void kblas_posv_vbatch_wsquery(kblasHandle_t h, const int max_n, int batchCount) {
   if (!h) return;
   KBlasWorkspaceState need;
-  need.d_data_bytes = kgb::vbatch_workspace_bytes(max_n, batchCount);
+  const size_t a = kgb::vbatch_ws_bytes(h, max_n, batchCount, true);
+  const size_t b = kgb::vbatch_ws_bytes(h, max_n, batchCount, false);
+  need.d_data_bytes = a > b ? a : b;
   h->ws.requested.pad(need);
 }
 

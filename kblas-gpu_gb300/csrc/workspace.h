@@ -1,23 +1,13 @@
-// workspace.h -- device workspace layout of the routines that need one.
+// workspace.h -- device workspace needs of the routines that have one (the
+// persistent mixed-precision and variable-size POSV); defined beside them.
 #pragma once
 #include <stddef.h>
 
+struct KBlasHandle;
+
 namespace kgb {
 
-static inline size_t ws_align(size_t x) { return (x + 255) / 256 * 256; }
-
-// Mixed-precision POSV: a queue header (counters) + a list of the systems
-// that take the FP64 fallback path.
-static inline size_t mixed_posv_workspace_bytes(char, int, int, int batch) {
-  if (batch <= 0) return 0;
-  return ws_align(64 * sizeof(int)) + ws_align((size_t)batch * sizeof(int));
-}
-
-// Variable-size POSV: the size-class histogram / offsets / queue counters,
-// the binned permutation of system indices, and the FP64 fallback list.
-static inline size_t vbatch_workspace_bytes(int, int batch) {
-  if (batch <= 0) return 0;
-  return ws_align(256 * sizeof(int)) + 2 * ws_align((size_t)batch * sizeof(int));
-}
+size_t mixed_posv_ws_bytes(KBlasHandle *h, int n, long long batch);
+size_t vbatch_ws_bytes(KBlasHandle *h, int max_n, long long batch, bool mixed);
 
 }  // namespace kgb
