@@ -285,7 +285,7 @@ def cpu_baseline(orc, wl, seconds_target=15.0, seed=0):
     rng = np.random.default_rng(seed + 1)
 
     def make(k):
-        pick = rng.choice(len(ns), k, replace=False)
+        pick = rng.choice(len(ns), k, replace=k > len(ns))
         As, Bs, nn = [], [], []
         for i in pick:
             n = int(ns[i])

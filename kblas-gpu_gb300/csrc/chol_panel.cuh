@@ -1,0 +1,539 @@
+// chol_panel.cuh -- team-level blocked Cholesky, triangular solves and FP64
+// residual on "panel" storage, for the persistent POSV kernels (n > 32).
+//
+// Storage of the lower triangle of one matrix of order n, block NB = 32:
+// panel p (J = 32 p) holds rows J..n-1 of columns J..J+jb-1 (jb = min(32,
+// n-J)), column-major with leading dimension ldp(p) = round_up(n - J, 4); the
+// panels follow each other. Columns are contiguous and 16-byte aligned, so
+// 4-row slices load as one 128-bit (FP32) or two 128-bit (FP64) accesses.
+//
+// Factorization (right-looking, one panel per step, 3 team barriers a step):
+//   (a) the 32 x 32 diagonal block is factored in registers by one warp,
+//       lane = row, columns broadcast by warp shuffles;
+//   (b) the rows below it are solved against it, one row per thread, the
+//       row held in registers and the block read as broadcast 128-bit loads
+//       from a row-major copy;
+//   (c) every later panel is updated with the new one: C -= P P^T, one 4 x 4
+//       register tile per thread and step of k, i.e. two 128-bit shared
+//       loads per 16 FMAs -- the one dense contraction of the factorization.
+#pragma once
+
+#include "device_util.cuh"
+#include "team.cuh"
+
+namespace kgb {
+
+constexpr int PNB = 32;  // panel width
+constexpr int LDD = 33;  // row stride of the diagonal-block copy (conflict free)
+
+struct PanelLayout {
+  int n, np;
+  __host__ __device__ __forceinline__ int jb(int p) const { return min(PNB, n - p * PNB); }
+  __host__ __device__ __forceinline__ int ldp(int p) const { return ((n - p * PNB) + 3) & ~3; }
+  // element offset of panel p (sum of the sizes of the panels before it)
+  __host__ __device__ __forceinline__ size_t base(int p) const {
+    // sum_{q<p} round4(n - 32 q) * 32 ; closed form would need the rounding of
+    // each term, a loop over <= 32 panels is cheap
+    size_t s = 0;
+    for (int q = 0; q < p; q++) s += (size_t)(((n - q * PNB) + 3) & ~3) * PNB;
+    return s;
+  }
+  __host__ __device__ __forceinline__ size_t total() const { return base(np); }
+};
+
+__host__ __device__ __forceinline__ PanelLayout make_layout(int n) {
+  PanelLayout L;
+  L.n = n;
+  L.np = (n + PNB - 1) / PNB;
+  return L;
+}
+
+// ----------------------------------------------------------------------------
+// Warp-register Cholesky of a jb x jb block (jb <= W <= 32), lane = row, in a
+// segment of W lanes. Row `lane` arrives in v[0..31] (columns 0..jb-1). The
+// column loop is rolled and the row registers rotate by one each step (the
+// current column is always v[0]), so the code stays small: this runs on one
+// warp while the rest of the team waits, and a fully unrolled 32 x 32 version
+// is instruction-fetch bound. Column c of L is written to Lrow[lane * ldr + c]
+// (row-major) and 1 / L(c,c) to rinv[c]. Every lane of the warp executes every
+// shuffle (jb is uniform across the warp's segments); a failed segment keeps
+// computing with a unit pivot, recording only its first failing column.
+template <typename T, int W, bool CHECK_INF>
+__device__ __forceinline__ int warp_chol_rot(T (&v)[32], int jb, T tol, T *Lrow, int ldr, T *rinv)
+{
+  const int lane = threadIdx.x & (W - 1);
+  int fail = 0;
+  for (int c = 0; c < jb; c++) {
+    const T d = __shfl_sync(0xffffffffu, v[0], c, W);
+    const bool ok = (d > tol) && (!CHECK_INF || d < T(INFINITY));
+    if (!ok && fail == 0) fail = c + 1;
+    T s, r;
+    pivot_rs(ok ? d : T(1), s, r);
+    const T l = (lane == c) ? s : v[0] * r;  // L(lane, c) for lane >= c
+    if (lane >= c && lane < jb) Lrow[lane * ldr + c] = l;
+    if (lane == c) rinv[c] = r;
+#pragma unroll
+    for (int k = 1; k < W; k++) {
+      const T lk = __shfl_sync(0xffffffffu, l, (c + k) & (W - 1), W);  // L(c+k, c)
+      if (lane >= c + k) v[k] -= l * lk;
+    }
+#pragma unroll
+    for (int k = 1; k < W; k++) v[k - 1] = v[k];
+    v[W - 1] = T(0);
+  }
+  return fail;
+}
+
+// ----------------------------------------------------------------------------
+// Panel Cholesky of the team's matrix. Ps: panel storage (shared or global).
+// Ld: 32 x 32 row-major scratch (shared) for the current diagonal block.
+// rinv: n reciprocal pivots. flag: one int of team-shared scratch.
+// Returns 1-based failing column or 0.
+// INV: the diagonal 32 x 32 square of each panel receives the inverse of
+// L_JJ instead of L_JJ (lower part), and its transpose in the strict upper
+// part, so the triangular solves become two small matrix-vector products per
+// panel (used by the FP32 refinement solves).
+template <typename T, bool CHECK_INF, bool INV = false>
+__device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *Ld, T *rinv, T tol,
+                                int *flag, bool active)
+{
+  if (!active) return 0;
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  int fail = 0;
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    T *Pp = Ps + L.base(p);
+    // (a) diagonal block, warp 0, lane = row: L -> Ld (row-major), then -> panel
+    if (w == 0) {
+      T v[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
+      const int f = warp_chol_rot<T, 32, CHECK_INF>(v, jb, tol, Ld, LDD, rinv + J);
+      __syncwarp();
+      if (!INV) {
+        // write L_JJ back column by column (coalesced in the panel)
+        for (int c = 0; c < jb; c++)
+          if (lane >= c && lane < jb) Pp[lane + c * ld] = Ld[lane * LDD + c];
+      } else {
+        // lane j computes column j of X = L_JJ^{-1} by forward substitution
+        // (X[k] = 0 above the diagonal), then X goes to the lower part and
+        // X^T to the strict upper part of the diagonal square
+        T X[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) X[k] = T(0);
+        for (int i = 0; i < jb; i++) {
+          T s = (i == lane) ? T(1) : T(0);
+          const T *li = Ld + i * LDD;
+#pragma unroll
+          for (int k = 0; k < 32; k++)
+            if (k < i) s -= li[k] * X[k];
+          const T xi = s * rinv[J + i];
+#pragma unroll
+          for (int k = 0; k < 32; k++)
+            if (k == i) X[k] = xi;
+        }
+        __syncwarp();
+        if (lane < jb) {
+#pragma unroll
+          for (int k = 0; k < 32; k++) {
+            if (k < jb) {
+              // X[k] = Xinv(k, lane): lower entry (k, lane) and mirrored (lane, k)
+              if (k >= lane) Pp[k + lane * ld] = X[k];
+              if (k > lane) Pp[lane + k * ld] = X[k];
+            }
+          }
+        }
+      }
+      if (lane == 0) *flag = f ? J + f : 0;
+    }
+    t.sync();
+    fail = *flag;
+    if (fail) break;
+    // (b) rows below the diagonal block: x * L_JJ^T = p
+    const int rows = L.n - J;
+    for (int i = jb + t.tid; i < rows; i += t.nt) {
+      T x[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) x[c] = (c < jb) ? Pp[i + c * ld] : T(0);
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        if (c < jb) {
+          T s0 = x[c], s1 = T(0);
+          const T *lrow = Ld + c * LDD;
+#pragma unroll
+          for (int q = 0; q < 32; q++) {
+            if (q < c) {
+              if (q & 1) s1 -= x[q] * lrow[q];
+              else s0 -= x[q] * lrow[q];
+            }
+          }
+          const T s = s0 + s1;
+          x[c] = s * rinv[J + c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < jb) Pp[i + c * ld] = x[c];
+    }
+    t.sync();
+    // (c) trailing update of every later panel with this one, 4 x 4 tiles
+    {
+      // count tiles per later panel: row tiles ceil(mq/4) x col tiles jbq/4 (jbq rounded up)
+      int tile0 = 0;
+      for (int q = p + 1; q < L.np; q++) {
+        const int K = q * PNB, mq = L.n - K, jq = L.jb(q);
+        const int rt = (mq + 3) >> 2, ct = (jq + 3) >> 2;
+        const int ntile = rt * ct;
+        T *Pq = Ps + L.base(q);
+        const int ldq = L.ldp(q);
+        const int start = ((t.tid - tile0) % t.nt + t.nt) % t.nt;
+        for (int tt = start; tt < ntile; tt += t.nt) {
+          const int c4 = tt / rt, r4 = tt - c4 * rt;
+          const int i0 = r4 * 4, c0 = c4 * 4;  // rows K+i0.., cols c0.. of panel q
+          if (i0 + 3 < c0) continue;           // entirely above the diagonal
+          T acc[4][4];
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+          const T *arow = Pp + (K - J) + i0;   // rows K+i0..K+i0+3 of panel p
+          const T *brow = Pp + (K - J) + c0;   // rows K+c0..K+c0+3 of panel p
+          for (int k = 0; k < jb; k++) {
+            T a[4], b[4];
+            if (sizeof(T) == 4) {
+              const float4 av = *reinterpret_cast<const float4 *>(arow + (size_t)k * ld);
+              const float4 bv = *reinterpret_cast<const float4 *>(brow + (size_t)k * ld);
+              a[0] = av.x; a[1] = av.y; a[2] = av.z; a[3] = av.w;
+              b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
+            } else {
+              const double2 a01 = *reinterpret_cast<const double2 *>(arow + (size_t)k * ld);
+              const double2 a23 = *reinterpret_cast<const double2 *>(arow + (size_t)k * ld + 2);
+              const double2 b01 = *reinterpret_cast<const double2 *>(brow + (size_t)k * ld);
+              const double2 b23 = *reinterpret_cast<const double2 *>(brow + (size_t)k * ld + 2);
+              a[0] = a01.x; a[1] = a01.y; a[2] = a23.x; a[3] = a23.y;
+              b[0] = b01.x; b[1] = b01.y; b[2] = b23.x; b[3] = b23.y;
+            }
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+              for (int y = 0; y < 4; y++) acc[x][y] += a[x] * b[y];
+          }
+#pragma unroll
+          for (int y = 0; y < 4; y++) {
+            if (c0 + y < jq) {
+              T *col = Pq + (size_t)(c0 + y) * ldq + i0;
+#pragma unroll
+              for (int x = 0; x < 4; x++) col[x] -= acc[x][y];  // padding rows absorb the overhang
+            }
+          }
+        }
+        tile0 += ntile;
+      }
+    }
+    t.sync();
+  }
+  (void)lane;
+  (void)nw;
+  return fail;
+}
+
+// ----------------------------------------------------------------------------
+// y := L^{-T} L^{-1} y on panel storage (team of whole warps). red: nw * 32
+// team-shared scratch.
+// Sum over the 32 lanes of a warp for each of 32 columns at once: on entry
+// lane i holds v[j] (contribution of lane i to column j); on exit lane j holds
+// sum_i v[j]. Five butterfly rounds, 31 shuffles and 31 adds in total.
+template <typename T>
+__device__ __forceinline__ T warp_transpose_sum32(T (&v)[32])
+{
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int lvl = 16; lvl >= 1; lvl >>= 1) {
+    const bool hi = (lane & lvl) != 0;
+#pragma unroll
+    for (int k = 0; k < lvl; k++) {
+      const T send = hi ? v[k] : v[k + lvl];
+      const T keep = hi ? v[k + lvl] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, lvl);
+    }
+  }
+  return v[0];
+}
+
+// y := L^{-T} L^{-1} y on panel storage (team of whole warps). red: nw * 32
+// team-shared scratch.
+//  forward, per panel: one warp sweeps the 32 x 32 diagonal block with its
+//    row of L preloaded in registers (32 dependent steps of one shuffle and
+//    one FMA), then each thread updates one row below (coalesced);
+//  backward, per panel (last first): the off-diagonal products are summed per
+//    column with lanes running down the rows (conflict-free reads) and one
+//    warp transpose-sum, then one warp sweeps the diagonal block.
+template <typename T, bool INV = false>
+__device__ void team_llt_solve_panel(const Team &t, const PanelLayout &L, const T *Ps,
+                                     const T *rinv, T *y, T *red, bool active)
+{
+  if (!active) return;
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    if (INV && w == 0) {
+      // y_J := L_JJ^{-1} y_J: lane i takes row i of the inverse (lower part)
+      T v0 = T(0), v1 = T(0);
+      if (lane < jb) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          if (k <= lane && k < jb) v0 += Pp[lane + k * ld] * y[J + k];
+          if (k + 1 <= lane && k + 1 < jb) v1 += Pp[lane + (k + 1) * ld] * y[J + k + 1];
+        }
+      }
+      __syncwarp();
+      if (lane < jb) y[J + lane] = v0 + v1;
+    } else if (w == 0) {
+      T lr[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) lr[c] = (c < lane && lane < jb) ? Pp[lane + c * ld] : T(0);
+      T v = (lane < jb) ? y[J + lane] : T(0);
+      const T ri = (lane < jb) ? rinv[J + lane] : T(0);
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        if (c < jb) {
+          if (lane == c) v *= ri;
+          const T yc = __shfl_sync(0xffffffffu, v, c);
+          v -= lr[c] * yc;  // lr[c] = 0 unless lane > c
+        }
+      }
+      if (lane < jb) y[J + lane] = v;
+    }
+    t.sync();
+    for (int i = jb + t.tid; i < L.n - J; i += t.nt) {
+      T s0 = T(0), s1 = T(0);
+#pragma unroll 4
+      for (int c = 0; c < jb; c += 2) {
+        s0 += Pp[i + c * ld] * y[J + c];
+        if (c + 1 < jb) s1 += Pp[i + (c + 1) * ld] * y[J + c + 1];
+      }
+      y[J + i] -= s0 + s1;
+    }
+    t.sync();
+  }
+  for (int p = L.np - 1; p >= 0; p--) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    // partial[c] = sum over rows i >= J+jb of L(i, J+c) * y_i: warp w takes
+    // row chunks w, w+nw, ... of 32 rows; lane = row
+    T acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++) acc[c] = T(0);
+    for (int i0 = jb + w * 32; i0 < L.n - J; i0 += nw * 32) {
+      const int i = i0 + lane;
+      const T yi = (i < L.n - J) ? y[J + i] : T(0);
+      const T *row = Pp + min(i, ld - 1);
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < jb) acc[c] += row[(size_t)c * ld] * yi;
+    }
+    const T part = warp_transpose_sum32<T>(acc);
+    red[w * 32 + lane] = part;
+    t.sync();
+    if (INV && w == 0) {
+      // x_J := L_JJ^{-T} (y_J - partials): row i of the strict upper part
+      // holds column i of the inverse
+      T sv = (lane < jb) ? y[J + lane] : T(0);
+      for (int q = 0; q < nw; q++) sv -= red[q * 32 + lane];
+      if (lane < jb) y[J + lane] = sv;
+      __syncwarp();
+      T v0 = T(0), v1 = T(0);
+      if (lane < jb) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          if (k >= lane && k < jb) v0 += Pp[lane + k * ld] * y[J + k];
+          if (k + 1 >= lane && k + 1 < jb) v1 += Pp[lane + (k + 1) * ld] * y[J + k + 1];
+        }
+      }
+      __syncwarp();
+      if (lane < jb) y[J + lane] = v0 + v1;
+    } else if (w == 0) {
+      T lc[32];  // column `lane` of L_JJ: lc[c] = L(J+c, J+lane) for c > lane
+#pragma unroll
+      for (int c = 0; c < 32; c++) lc[c] = (c > lane && c < jb) ? Pp[c + lane * ld] : T(0);
+      T v = (lane < jb) ? y[J + lane] : T(0);
+      for (int q = 0; q < nw; q++) v -= red[q * 32 + lane];
+      const T ri = (lane < jb) ? rinv[J + lane] : T(0);
+#pragma unroll
+      for (int c = 31; c >= 0; c--) {
+        if (c < jb) {
+          if (lane == c) v *= ri;
+          const T xc = __shfl_sync(0xffffffffu, v, c);
+          v -= lc[c] * xc;  // lc[c] = 0 unless c > lane
+        }
+      }
+      if (lane < jb) y[J + lane] = v;
+    }
+    t.sync();
+  }
+}
+
+// Stage the lower triangle of A (FP64, column-major, lda) into panel storage
+// of type T. SCALE: FP32 value (float)a_ij * scl[i] * scl[j]. Padding rows and
+// the strict upper part of each diagonal block are zeroed.
+// Stage the lower triangle of A (FP64, column-major, lda) into panel storage
+// of type T (SCALE: FP32 (float)a_ij * scl[i] * scl[j]). One thread per panel
+// row issues the 32 loads of the row before using any (32 loads in flight).
+// Padding rows and the strict upper part of each diagonal block get zeros.
+// rowabs (may be NULL): rowabs[i] += sum_j |a_ij| over the whole symmetric
+// row, accumulated with shared-memory atomics (row part in the thread, the
+// mirrored column part by a warp transpose-sum), for ||A||_inf.
+template <typename T, bool SCALE>
+__device__ void team_load_panels(const Team &t, const PanelLayout &L, const double *__restrict__ A,
+                                 int lda, T *Ps, const float *scl, float *rowabs)
+{
+  const int lane = t.lane();
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    T *Pp = Ps + L.base(p);
+    const int rows = (ld + 31) & ~31;  // whole warps stay together for the column sums
+    for (int ii = t.tid; ii < rows; ii += t.nt) {
+      const int i = J + ii;
+      const bool in = ii < ld;        // a row of the panel (padding rows get zeros)
+      const bool real = i < L.n;      // a row of the matrix
+      const float si = (SCALE && real) ? scl[i] : 1.0f;
+      float rsum = 0.f;
+#pragma unroll
+      for (int h = 0; h < 32; h += 16) {
+        double a[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++)
+          a[c] = (real && h + c < jb && ii >= h + c) ? A[(size_t)i + (size_t)(J + h + c) * lda] : 0.0;
+        float cabs[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+          const float af = (float)a[c];
+          if (in && h + c < jb) {
+            T v;
+            if (SCALE) v = (T)(af * si * scl[J + h + c]);
+            else v = (T)a[c];
+            Pp[ii + (h + c) * ld] = v;
+          }
+          rsum += fabsf(af);
+          cabs[c] = (ii > h + c) ? fabsf(af) : 0.f;  // strictly lower: mirrored into row J+h+c
+        }
+        if (rowabs) {
+          // column sums over the warp's 32 rows: lanes 0..15 end with columns h..h+15
+          float cs = 0.f;
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            float v = cabs[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == c) cs = v;
+          }
+          if (lane < 16 && h + lane < jb) atomicAdd(&rowabs[J + h + lane], cs);
+        }
+      }
+      if (rowabs && real) atomicAdd(&rowabs[i], rsum);
+    }
+  }
+}
+
+// Write the factor held in panel storage back to A's lower triangle (columns
+// 0..ncol-1).
+template <typename T>
+__device__ void team_store_panels(const Team &t, const PanelLayout &L, const T *Ps, double *A,
+                                  int lda, int ncol)
+{
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    if (J >= ncol) break;
+    const T *Pp = Ps + L.base(p);
+    const int rows = L.n - J;
+    const int cols = min(jb, ncol - J);
+    for (int e = t.tid; e < rows * cols; e += t.nt) {
+      const int c = e / rows, ii = e - c * rows;
+      if (ii >= c) A[(size_t)(J + ii) + (size_t)(J + c) * lda] = (double)Pp[ii + c * ld];
+    }
+  }
+}
+
+// FP64 residual of up to MR right-hand sides of X*A = B: r_q = b_q - A x_q, A
+// symmetric from its lower triangle (global memory). One row per thread,
+// loads unrolled by 4 so several are in flight.
+// FP64 residual r = b - A x for one right-hand side, A symmetric from its
+// lower triangle (global memory, column-major), cut into 32 x 32 tiles. Warp
+// w takes the block columns Jb = w, w + nw, ...; walking down block column
+// Jb, lane i loads row i of tile (I, Jb) (32 independent coalesced loads),
+// adds a_ij x_j to the row sum of row I+i (kept per warp in shared memory),
+// and accumulates the mirrored products a_ij x_i per column j in registers;
+// one transpose-sum per block column turns those into the column sums. Every
+// element costs exactly its two FMAs of the symmetric product; the adds of
+// the transpose-sum are spread over a whole block column.
+// rowsum: nw x n doubles of team-shared scratch.
+static __device__ void team_residual_tiled(const Team &t, int n, const double *__restrict__ A,
+                                           int lda, const double *__restrict__ b, int incb,
+                                           const double *x, double *r, double *rowsum,
+                                           bool active)
+{
+  if (!active) return;
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  const int nb = (n + 31) / 32;
+  const int ntile = nb * (nb + 1) / 2;
+  // tiles in column-major order (block column Jb, then rows I >= Jb); warp w
+  // takes a contiguous, equal share, so it touches one or two block columns
+  const int t0 = (int)((long long)ntile * w / nw), t1 = (int)((long long)ntile * (w + 1) / nw);
+  double *mine = rowsum + (size_t)w * n;
+  for (int i = lane; i < n; i += 32) mine[i] = 0.0;
+  __syncwarp();
+  int Jb = 0, first = 0;  // first tile index of block column Jb
+  while (first + (nb - Jb) <= t0) {
+    first += nb - Jb;
+    Jb++;
+  }
+  int tt = t0;
+  while (tt < t1) {
+    const int J0 = Jb * 32;
+    const int Ibeg = Jb + (tt - first), Iend = min(nb, Jb + (t1 - first));
+    const double *xj = x + J0;
+    double mir[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) mir[j] = 0.0;
+    for (int I = Ibeg; I < Iend; I++) {
+      const int row = I * 32 + lane;
+      const bool rin = row < n;
+      const double xi = rin ? x[row] : 0.0;
+      double rs0 = 0.0, rs1 = 0.0;
+#pragma unroll
+      for (int h = 0; h < 32; h += 16) {
+        double a[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int jj = h + j;
+          const bool ok = rin && J0 + jj < n && (I > Jb || jj <= lane);
+          a[j] = ok ? A[(size_t)row + (size_t)(J0 + jj) * lda] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j += 2) {
+          rs0 += a[j] * xj[min(h + j, n - 1 - J0)];
+          rs1 += a[j + 1] * xj[min(h + j + 1, n - 1 - J0)];
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (I > Jb || h + j < lane) mir[h + j] += a[j] * xi;  // strictly lower entries only
+      }
+      if (rin) mine[row] += rs0 + rs1;
+    }
+    const double cs = warp_transpose_sum32<double>(mir);
+    if (J0 + lane < n) mine[J0 + lane] += cs;
+    tt += Iend - Ibeg;
+    first += nb - Jb;
+    Jb++;
+  }
+  t.sync();
+  for (int i = t.tid; i < n; i += t.nt) {
+    double s = 0.0;
+    for (int q = 0; q < nw; q++) s += rowsum[(size_t)q * n + i];
+    r[i] = b[(size_t)i * incb] - s;
+  }
+  t.sync();
+}
+
+}  // namespace kgb

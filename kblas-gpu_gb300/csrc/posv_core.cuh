@@ -3,42 +3,45 @@
 // (kblasDposv_vbatch*) entry points.
 //
 // One launch processes a whole batch. CTAs pull work items from a device
-// queue (one atomicAdd per item, no waiting anywhere). A work item is a group
-// of systems of the same order n; the CTA's threads are split into teams of
-// TS threads, one system per team (TS and the systems per item come from the
-// tuning table, per size class). Per system, everything happens while the
-// system is on chip -- read A once, factor, solve, refine, write X:
+// queue (one atomicAdd per item; nothing ever waits on another CTA). A work
+// item is a group of systems of the same order n; the CTA's threads are
+// split into teams of TS threads, one system per team (TS and the systems per
+// item come from the tuning table, per size class). Per system, everything
+// happens while the system is on chip -- read A, factor, solve, refine,
+// write X:
 //
 //  MIXED (X*A = B, side 'R', lower; LAPACK DSPOSV semantics):
-//   1. stage A's lower triangle as FP32 with power-of-two symmetric diagonal
-//      scaling  As = S A S,  S = diag(2^-e_i),  e_i = floor(log2(a_ii) / 2),
-//      so the factor stays in range (the scaling is exact);
-//   2. FP32 Cholesky As = Ls Ls^T in shared memory (pivot test d > n*2^-24);
-//   3. x = S Ls^-T Ls^-1 S b in FP32, then refine: r = b - A x in FP64 (A
-//      re-read from L2), stop when ||r|| <= 2 sqrt(n) eps64 (||A|| ||x|| +
-//      ||b||) -- with the residual's own rounding this certifies a backward
-//      error below 10 n eps64 -- else x += S Ls^-T Ls^-1 S r (FP32 solve,
-//      FP64 update);
+//   1. power-of-two symmetric diagonal scaling As = S A S, S = diag(2^-e_i),
+//      e_i = floor(log2(a_ii)/2): exact, and keeps the FP32 factor in range;
+//   2. FP32 Cholesky As = Ls Ls^T on chip (pivot test d > n*2^-24);
+//   3. x = S Ls^-T Ls^-1 S b in FP32, then refinement: r = b - A x in FP64 (A
+//      re-read, L2 resident), stop when ||r|| <= 2 sqrt(n) eps64 (||A|| ||x|| +
+//      ||b||) -- with the residual's own rounding (< (n+1) eps64) this
+//      certifies a normwise backward error below 10 n eps64 -- else
+//      x += S Ls^-T Ls^-1 S r (FP32 solve, FP64 update);
 //   4. a system whose FP32 factorization fails, or whose refinement stalls
 //      (error not halved) or runs out of steps, is factored again in FP64 by
-//      the same team (packed factor in a global scratch slot) and solved
-//      directly; A then receives the FP64 factor and info the exact LAPACK
-//      code. iter[] records the outcome.
-//  PLAIN (FP64 POSV): FP64 factor in shared memory (or the scratch slot when
-//   it does not fit), solve, write L and X -- LAPACK DPOSV semantics.
+//      the same team and solved directly; A then receives the FP64 factor and
+//      info the exact LAPACK code; iter[] records which path was taken.
+//  PLAIN (FP64 POSV): FP64 factor, solve, write L and X (LAPACK DPOSV).
+//
+// n <= 32: register path (chol_small.cuh), W lanes per system (W >= n).
+// n >  32: panel path (chol_panel.cuh), teams of whole warps; the factor in
+//          shared memory, or in the CTA's global scratch slot when too big.
 #pragma once
 
 #include <stdint.h>
 
-#include "chol_dev.cuh"
+#include "chol_small.cuh"
 #include "team.cuh"
 
 namespace kgb {
 
 constexpr int PC_NT = 256;     // threads per persistent CTA
 constexpr int PC_NCLS = 6;     // size classes
-constexpr int PC_MR = 4;       // right-hand sides per residual sweep
+constexpr int PC_MR = 4;       // right-hand sides per residual sweep (panel path)
 constexpr int PC_ITMAX = 12;   // refinement step cap
+constexpr double PC_EPS64 = 1.1102230246251565e-16;
 
 struct PosvCfg {
   int nmax[PC_NCLS];  // class c holds n <= nmax[c] (ascending)
@@ -52,8 +55,7 @@ __host__ __device__ __forceinline__ int pc_class(const PosvCfg &c, int n) {
   return PC_NCLS - 1;
 }
 
-// Describes where the systems are: uniform strided / pointer-array, or
-// per-system arrays (variable size). All pointers are device pointers.
+// Where the systems are: uniform strided / pointer array, or per-system arrays.
 struct SysArgs {
   int mode;  // 0 uniform strided, 1 uniform pointer array, 2 variable size
   int n, m, lda, ldb;
@@ -64,273 +66,370 @@ struct SysArgs {
   double *const *Aarr;
   double *const *Barr;
   const int *narr, *marr, *ldaarr, *ldbarr;
-  __device__ __forceinline__ void get(long long b, int &nn, int &mm, double *&Ap, int &la,
-                                      double *&Bp, int &lb) const {
+  __device__ __forceinline__ void get(long long b, int &mm, double *&Ap, int &la, double *&Bp,
+                                      int &lb) const {
     if (mode == 2) {
-      nn = narr[b]; mm = marr[b]; la = ldaarr[b]; lb = ldbarr[b];
+      mm = marr[b]; la = ldaarr[b]; lb = ldbarr[b];
       Ap = Aarr[b]; Bp = Barr[b];
     } else {
-      nn = n; mm = m; la = lda; lb = ldb;
+      mm = m; la = lda; lb = ldb;
       Ap = (mode == 0) ? A + b * sA : Aarr[b];
       Bp = (mode == 0) ? B + b * sB : Barr[b];
     }
   }
 };
 
-// Work items: uniform batches are cut into consecutive groups; binned
-// variable-size batches use the item table written by the binning kernels.
 struct ItemArgs {
   int uniform;          // 1: item q = systems [q*spi, (q+1)*spi)
   long long batch;
   int n_uniform;
   const int4 *items;    // (n, start, count, -) into perm
   const int *perm;
-  const int *nitems_p;  // number of items (device), for binned batches
+  const int *nitems_p;  // number of items (device), binned batches
   int *queue;           // work counter (zeroed before the launch)
 };
 
 struct OutArgs {
-  int *info;   // may be NULL
-  int *iter;   // may be NULL (mixed only)
+  int *info;
+  int *iter;
   char *scratch;         // per-CTA global scratch slots
-  long long slot_bytes;  // bytes per CTA slot
+  long long slot_bytes;
 };
 
-// ---- per-team shared memory layout -------------------------------------
+// ---------------------------------------------------------------------------
+// shared-memory bytes of one team
+// ---------------------------------------------------------------------------
 template <bool MIXED>
-__host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool lp_in_smem) {
-  const size_t P = (size_t)n * (n + 1) / 2;
-  const int nw = ts >= 32 ? ts / 32 : 1;
-  size_t b = 0;
-  if (MIXED) {
-    b += (lp_in_smem ? P : 0) * 4;        // FP32 factor
-    b += 3 * (size_t)n * 4;               // rinv, scale, (spare)
-    b += (size_t)PC_MR * n * 4;           // FP32 solve vectors
-    b = (b + 7) / 8 * 8;
-    b += 2 * (size_t)PC_MR * n * 8;       // x, r (FP64)
-    b += (size_t)32 * nw * 8;             // reduction scratch
-    b += 64;                              // flags
-  } else {
-    b += (lp_in_smem ? P : 0) * 8;        // FP64 factor
-    b += (size_t)n * 8;                   // rinv
-    b += (size_t)PC_MR * n * 8;           // solve vectors
-    b += (size_t)32 * nw * 8;
-    b += 64;
+__host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool fac_in_smem) {
+  if (n <= 32) {
+    // register path: row-major L (FP64; FP32 too for mixed), reciprocal
+    // pivots, scales
+    const int W = ts;
+    size_t b = (size_t)W * (W + 1) * 8 + (size_t)W * 8;
+    if (MIXED) b += (size_t)W * (W + 1) * 4 + 2 * (size_t)W * 4;
+    return (b + 15) / 16 * 16;
   }
+  const PanelLayout L = make_layout(n);
+  const int nw = ts / 32;
+  const size_t T = MIXED ? 4 : 8;
+  size_t b = 0;
+  b += (fac_in_smem ? L.total() : 0) * T;          // panels
+  b += 32 * LDD * 8;                               // diagonal block (FP64 size: fallback too)
+  b += (size_t)n * 8;                              // rinv (FP64 size: fallback too)
+  if (MIXED) {
+    b += (size_t)n * 4;                            // scales
+    b += (size_t)PC_MR * n * 4;                    // FP32 solve vectors
+    b = (b + 7) / 8 * 8;
+    b += 2 * (size_t)PC_MR * n * 8;                // x, r
+    b += (size_t)nw * n * 8;                       // per-warp column sums of the residual
+  } else {
+    b += (size_t)n * 8;                            // solve vector
+  }
+  b += (size_t)32 * nw * 8;                        // reductions / partial sums
+  b += 16;                                         // flag
   return (b + 15) / 16 * 16;
 }
 
-// Stage A's lower triangle (FP64) into the packed factor storage of type T,
-// optionally as FP32 with the exponent shifts e[] applied.
-template <typename T, bool SCALE>
-__device__ __forceinline__ void team_load_lower(const Team &t, int n, const double *A, int lda,
-                                                T *Lp, const float *scl)
-{
-  // columns one after the other, team lanes along the rows (coalesced)
-  for (int k = 0; k < n; k++) {
-    const double *col = A + (size_t)k * lda;
-    T *dst = Lp + coff(k, n) - k;
-    for (int i = k + t.tid; i < n; i += t.nt) {
-      if (SCALE) dst[i] = (T)((float)col[i] * scl[i] * scl[k]);
-      else dst[i] = (T)col[i];
-    }
-  }
-}
-
-// Loop bound that is uniform across every team sharing a warp: sub-warp
-// teams must call the same sequence of __syncwarp, so loops whose trip count
-// depends on per-system data run to the warp-wide maximum.
-__device__ __forceinline__ int warp_uniform_max(const Team &t, int v) {
-  if (t.nt >= 32) return v;
+// ---------------------------------------------------------------------------
+// helpers keeping sub-warp teams in step
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int warp_uniform_max_w(int v, int W) {
+  if (W >= 32) return v;
   for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
-__device__ __forceinline__ int group_any(const Team &t, int v, int *scratch) {
-  if (t.nt < 32) return __any_sync(0xffffffffu, v);  // warp-wide: keeps sub-warp teams in step
-  return team_any(t, v, scratch);
+__device__ __forceinline__ int seg_any(int v, int W) {
+  const unsigned ball = __ballot_sync(0xffffffffu, v);
+  if (W >= 32) return ball != 0u;
+  const int base = (threadIdx.x & 31) & ~(W - 1);
+  return ((ball >> base) & ((1u << W) - 1u)) != 0u;
 }
 
-// FP64 factor + solve of one system (the plain path, and the mixed path's
-// fallback). Lp64 is packed FP64 storage (shared or scratch). Solves the RHS
-// rows [r_from, m) of B and writes L to A. Returns the info code.
-static __device__ int team_fp64_posv(const Team &t, bool active, int n, int m, int r_from, double *A,
-                              int lda, double *B, int ldb, double *Lp64, double *rinv64, double *y,
-                              double *red)
-{
-  if (active) team_load_lower<double, false>(t, n, A, lda, Lp64, nullptr);
-  t.sync();
-  int info = team_potrf_packed<double>(t, n, Lp64, rinv64, 0.0, active);
-  // write the factor back (columns before a failure are the true factor; the
-  // failing column keeps its non-positive pivot, LAPACK xPOTRF style)
-  if (active) {
-    const int ncol = info ? info : n;
-    for (int k = 0; k < ncol; k++) {
-      double *col = A + (size_t)k * lda;
-      const double *src = Lp64 + coff(k, n) - k;
-      for (int i = k + t.tid; i < n; i += t.nt) col[i] = src[i];
+// power-of-two scale of row i from the FP64 diagonal; bad = outside FP32 range
+__device__ __forceinline__ float pow2_scale(double d, int &bad) {
+  if (d > 0.0 && d < 1e300) {
+    int e = ilogb(d);
+    e = (e >= 0) ? e / 2 : -((-e + 1) / 2);  // floor(log2(d) / 2)
+    if (e > 120 || e < -120) {
+      bad = 1;
+      return 1.0f;
     }
+    return ldexpf(1.0f, -e);
   }
-  const bool solve = active && info == 0;
-  const int m_hi = warp_uniform_max(t, active ? m : 0);
+  bad = 1;  // non-positive / NaN / huge diagonal: the FP64 path decides
+  return 1.0f;
+}
+
+// ===========================================================================
+// register path (n <= W <= 32); every segment of a warp runs every shuffle
+// ===========================================================================
+
+// FP64 factor + solve of RHS rows [r_from, m) -- plain path and fallback.
+// Ls64: W x (W+1) doubles, rinv64: W doubles (segment-private shared).
+template <int W>
+__device__ int small_fp64_posv(bool active, int n, int m, int r_from, double *A, int lda, double *B,
+                               int ldb, double *Ls64, double *rinv64)
+{
+  const int lane = threadIdx.x & (W - 1);
+  double v[32];
+  small_load<double, W, false>(n, active ? A : nullptr, lda, 1.0f, active, v);
+  const int fail = warp_chol_rot<double, W, false>(v, n, 0.0, Ls64, W + 1, rinv64);
+  __syncwarp();
+  if (active && lane < n) {
+    const int ncol = fail ? fail - 1 : n;
+    for (int c = 0; c <= lane && c < ncol; c++) A[(size_t)lane + (size_t)c * lda] = Ls64[lane * (W + 1) + c];
+  }
+  const bool solve = active && !fail;
+  const int m_hi = warp_uniform_max_w(active ? m : 0, W);
   for (int r0 = r_from; r0 < m_hi; r0++) {
     const bool go = solve && r0 < m;
-    if (go)
-      for (int i = t.tid; i < n; i += t.nt) y[i] = B[(size_t)r0 + (size_t)i * ldb];
-    t.sync();
-    team_llt_solve<double>(t, n, Lp64, rinv64, y, red, go);
-    if (go)
-      for (int i = t.tid; i < n; i += t.nt) B[(size_t)r0 + (size_t)i * ldb] = y[i];
-    t.sync();
+    double y = (go && lane < n) ? B[(size_t)r0 + (size_t)lane * ldb] : 0.0;
+    y = small_llt_solve<double, W>(n, Ls64, rinv64, y);
+    if (go && lane < n) B[(size_t)r0 + (size_t)lane * ldb] = y;
   }
-  return info;
+  __syncwarp();
+  return fail;
 }
 
-// Mixed-precision solve of one system by one team (see the file header).
-static __device__ void team_mixed_posv(const Team &t, bool active, int n, int m, double *A, int lda,
-                                double *B, int ldb, unsigned char *base, bool lp_smem,
-                                float *Lp_scratch, double *Lp64_scratch, int *info_out,
-                                int *iter_out)
+template <int W>
+__device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, double *B, int ldb,
+                                 unsigned char *base, int *info_out, int *iter_out)
 {
-  const size_t P = (size_t)n * (n + 1) / 2;
-  float *Lp = lp_smem ? reinterpret_cast<float *>(base) : Lp_scratch;
-  unsigned char *p = base + (lp_smem ? P * 4 : 0);
-  float *rinv = reinterpret_cast<float *>(p); p += (size_t)n * 4;
-  float *scl = reinterpret_cast<float *>(p); p += (size_t)n * 4;
-  p += (size_t)n * 4;
-  float *ys = reinterpret_cast<float *>(p); p += (size_t)PC_MR * n * 4;
-  p = reinterpret_cast<unsigned char *>(((uintptr_t)p + 7) & ~(uintptr_t)7);
-  double *x = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
-  double *r = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
-  double *red = reinterpret_cast<double *>(p);
-
-  // ---- 1. power-of-two scaling from the FP64 diagonal ----
-  int bad_diag = 0;
-  if (active)
-    for (int i = t.tid; i < n; i += t.nt) {
-      const double d = A[(size_t)i + (size_t)i * lda];
-      int e = 0;
-      if (d > 0.0 && d < 1e300) {
-        e = ilogb(d);
-        e = (e >= 0) ? e / 2 : -((-e + 1) / 2);  // floor(log2(d) / 2)
-        if (e > 120 || e < -120) bad_diag = 1;   // outside FP32 range: FP64 path
-      } else {
-        bad_diag = 1;  // non-positive / NaN / huge diagonal: the FP64 path decides
-      }
-      scl[i] = bad_diag ? 1.0f : ldexpf(1.0f, -e);
-    }
-  t.sync();
-  // ---- 2. stage As = S A S in FP32 and factor it ----
-  if (active) team_load_lower<float, true>(t, n, A, lda, Lp, scl);
-  t.sync();
-  const float ftol = (float)n * 5.9604645e-08f;  // n * 2^-24
-  const int fail = team_potrf_packed<float>(t, n, Lp, rinv, ftol, active);
-  // ||A||_inf (= ||A||_1 by symmetry); an FP32 sum is enough for a threshold
-  double anorm = 0.0;
-  if (active) {
-    float rs_max = 0.f;
-    for (int i = t.tid; i < n; i += t.nt) {
-      float s = 0.f;
-      for (int j = 0; j <= i; j++) s += fabsf((float)A[(size_t)i + (size_t)j * lda]);
-      for (int j = i + 1; j < n; j++) s += fabsf((float)A[(size_t)j + (size_t)i * lda]);
-      rs_max = fmaxf(rs_max, s);
-    }
-    anorm = (double)rs_max * (1.0 + 1e-6 * n);
+  const int lane = threadIdx.x & (W - 1);
+  double *Ls64 = reinterpret_cast<double *>(base);
+  double *rinv64 = Ls64 + W * (W + 1);
+  float *Ls = reinterpret_cast<float *>(rinv64 + W);
+  float *rinv = Ls + W * (W + 1);
+  float *scl = rinv + W;
+  int bad = 0;
+  float sc = 1.0f;
+  if (active && lane < n) sc = pow2_scale(A[(size_t)lane + (size_t)lane * lda], bad);
+  scl[lane] = sc;
+  float v[32];
+  small_load<float, W, true>(n, active ? A : nullptr, lda, sc, active, v);
+  // ||A||_inf from the staged values (|a_ij| = |as_ij| / (s_i s_j), exact)
+#pragma unroll
+  for (int c = 0; c < W; c++)
+    if (c <= lane) Ls[lane * (W + 1) + c] = v[c];
+  __syncwarp();
+  float rs = 0.f;
+  if (lane < n) {
+    for (int c = 0; c <= lane; c++) rs += fabsf(Ls[lane * (W + 1) + c]) / scl[c];
+    for (int j = lane + 1; j < n; j++) rs += fabsf(Ls[j * (W + 1) + lane]) / scl[j];
+    rs /= sc;
   }
-  anorm = team_max<double>(t, anorm, red);
-  const int bad = team_any(t, active && (fail != 0 || bad_diag), reinterpret_cast<int *>(red));
-  bool need_fb = active && bad;
+  const double anorm = (double)warp_max_width(rs, W) * (1.0 + 1e-6 * n);
+  __syncwarp();
+  const int fail = warp_chol_rot<float, W, true>(v, n, (float)n * 5.9604645e-08f, Ls, W + 1, rinv);
+  __syncwarp();
+  const int any_bad = seg_any(bad, W);
+  bool need_fb = active && (fail != 0 || any_bad);
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
-  const double tol_conv = 2.0 * sqrt((double)n) * 1.1102230246251565e-16;
-
-  // ---- 3. solve and refine, PC_MR right-hand sides at a time ----
-  const int m_hi = warp_uniform_max(t, active ? m : 0);
-  for (int r0 = 0; r0 < m_hi; r0 += PC_MR) {
-    const int nr = (active && r0 < m) ? min(PC_MR, m - r0) : 0;
-    const bool go0 = active && !need_fb && nr > 0;
-    for (int q = 0; q < PC_MR; q++) {
-      const bool gq = go0 && q < nr;
-      if (gq)
-        for (int i = t.tid; i < n; i += t.nt)
-          ys[q * n + i] = (float)B[(size_t)(r0 + q) + (size_t)i * ldb] * scl[i];
-      t.sync();
-      team_llt_solve<float>(t, n, Lp, rinv, ys + q * n, reinterpret_cast<float *>(red), gq);
-      if (gq)
-        for (int i = t.tid; i < n; i += t.nt) x[q * n + i] = (double)(ys[q * n + i] * scl[i]);
-      t.sync();
-    }
+  const double tol_conv = 2.0 * sqrt((double)n) * PC_EPS64;
+  const int m_hi = warp_uniform_max_w(active ? m : 0, W);
+  for (int r0 = 0; r0 < m_hi; r0++) {
+    const bool go = active && !need_fb && r0 < m;
+    const double b = (go && lane < n) ? B[(size_t)r0 + (size_t)lane * ldb] : 0.0;
+    float y = small_llt_solve<float, W>(n, Ls, rinv, (float)b * sc);
+    double x = (double)(y * sc);
     double eta_prev = INFINITY;
-    bool going = go0, converged = false;
+    bool going = go, converged = false;
     int step = 0;
-    while (group_any(t, going, reinterpret_cast<int *>(red))) {
-      team_residual<PC_MR>(t, n, A, lda, B, ldb, r0, nr, x, n, r, going);
-      t.sync();
-      double eta = 0.0;
-      for (int q = 0; q < PC_MR; q++) {
-        double rm = 0.0, xm = 0.0, bm = 0.0;
-        if (going && q < nr)
-          for (int i = t.tid; i < n; i += t.nt) {
-            rm = fmax(rm, fabs(r[q * n + i]));
-            xm = fmax(xm, fabs(x[q * n + i]));
-            bm = fmax(bm, fabs(B[(size_t)(r0 + q) + (size_t)i * ldb]));
-          }
-        rm = team_max<double>(t, rm, red);
-        xm = team_max<double>(t, xm, red);
-        bm = team_max<double>(t, bm, red);
-        if (going && q < nr) {
-          const double den = anorm * xm + bm;
-          const double e = (den > 0.0) ? rm / den : (rm > 0.0 ? INFINITY : 0.0);
-          eta = (e > eta || e != e) ? e : eta;
-        }
-      }
+    while (__any_sync(0xffffffffu, going)) {
+      const double r = small_residual<W>(n, A, lda, b, x, going);
+      const double rm = warp_max_width(lane < n ? fabs(r) : 0.0, W);
+      const double xm = warp_max_width(lane < n ? fabs(x) : 0.0, W);
+      const double bm = warp_max_width(lane < n ? fabs(b) : 0.0, W);
       if (going) {
+        const double den = anorm * xm + bm;
+        const double eta = (den > 0.0) ? rm / den : (rm > 0.0 ? INFINITY : 0.0);
         if (eta <= tol_conv) {
           going = false;
           converged = true;
         } else if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) {
-          going = false;  // stalled, NaN, or out of steps
+          going = false;
+        } else {
+          eta_prev = eta;
         }
       }
-      for (int q = 0; q < PC_MR; q++) {
-        const bool gq = going && q < nr;
-        if (gq)
-          for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = (float)r[q * n + i] * scl[i];
-        t.sync();
-        team_llt_solve<float>(t, n, Lp, rinv, ys + q * n, reinterpret_cast<float *>(red), gq);
-        if (gq)
-          for (int i = t.tid; i < n; i += t.nt) x[q * n + i] += (double)(ys[q * n + i] * scl[i]);
-        t.sync();
-      }
+      y = small_llt_solve<float, W>(n, Ls, rinv, going ? (float)r * sc : 0.0f);
       if (going) {
-        eta_prev = eta;
+        x += (double)(y * sc);
         step++;
       }
     }
-    if (go0) {
+    if (go) {
       steps_used = max(steps_used, step);
       if (converged) {
-        for (int q = 0; q < nr; q++)
-          for (int i = t.tid; i < n; i += t.nt) B[(size_t)(r0 + q) + (size_t)i * ldb] = x[q * n + i];
+        if (lane < n) B[(size_t)r0 + (size_t)lane * ldb] = x;
       } else {
         need_fb = true;
         fb_code = (step >= PC_ITMAX) ? -3 : -2;
         fb_from = r0;
       }
     }
-    t.sync();
   }
-  // ---- 4. FP64 fallback for the systems that need it ----
   int info = 0;
-  if (group_any(t, need_fb, reinterpret_cast<int *>(red)))
-    info = team_fp64_posv(t, need_fb, n, m, fb_from, A, lda, B, ldb, Lp64_scratch, r, x, red);
-  if (active && t.tid == 0) {
+  if (__any_sync(0xffffffffu, need_fb))
+    info = small_fp64_posv<W>(need_fb, n, m, fb_from, A, lda, B, ldb, Ls64, rinv64);
+  if (active && lane == 0) {
     if (info_out) *info_out = need_fb ? info : 0;
     if (iter_out) *iter_out = need_fb ? fb_code : steps_used;
   }
 }
 
+// ===========================================================================
+// panel path (n > 32, teams of whole warps)
+// ===========================================================================
+
+// FP64 factor + solve of RHS rows [r_from, m). Ps64: panel storage (shared or
+// global scratch); Ld: 32x32 doubles; rinv, y: n doubles; red: 32 * nwarps
+// doubles; flag: one int.
+static __device__ int panel_fp64_posv(const Team &t, int n, int m, int r_from, double *A, int lda,
+                               double *B, int ldb, double *Ps64, double *Ld, double *rinv, double *y,
+                               double *red, int *flag)
+{
+  const PanelLayout L = make_layout(n);
+  team_load_panels<double, false>(t, L, A, lda, Ps64, nullptr, nullptr);
+  t.sync();
+  const int info = team_potrf_panel<double, false>(t, L, Ps64, Ld, rinv, 0.0, flag, true);
+  team_store_panels<double>(t, L, Ps64, A, lda, info ? info - 1 : n);
+  if (!info) {
+    for (int r0 = r_from; r0 < m; r0++) {
+      for (int i = t.tid; i < n; i += t.nt) y[i] = B[(size_t)r0 + (size_t)i * ldb];
+      t.sync();
+      team_llt_solve_panel<double>(t, L, Ps64, rinv, y, red, true);
+      for (int i = t.tid; i < n; i += t.nt) B[(size_t)r0 + (size_t)i * ldb] = y[i];
+      t.sync();
+    }
+  }
+  t.sync();
+  return info;
+}
+
+static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, int lda, double *B,
+                                 int ldb, unsigned char *base, bool fac_smem, float *Ps_scratch,
+                                 double *Ps64_scratch, int *info_out, int *iter_out)
+{
+  const PanelLayout L = make_layout(n);
+  const int nw = t.nwarps();
+  float *Ps = fac_smem ? reinterpret_cast<float *>(base) : Ps_scratch;
+  unsigned char *p = base + (fac_smem ? L.total() * 4 : 0);
+  double *Ld64 = reinterpret_cast<double *>(p); p += 32 * LDD * 8;
+  float *Ld = reinterpret_cast<float *>(Ld64);
+  double *rinv64 = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+  float *rinv = reinterpret_cast<float *>(rinv64);
+  float *scl = reinterpret_cast<float *>(p); p += (size_t)n * 4;
+  float *ys = reinterpret_cast<float *>(p); p += (size_t)PC_MR * n * 4;
+  p = reinterpret_cast<unsigned char *>(((uintptr_t)p + 7) & ~(uintptr_t)7);
+  double *x = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
+  double *r = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
+  double *colsum = reinterpret_cast<double *>(p); p += (size_t)nw * n * 8;
+  double *red = reinterpret_cast<double *>(p); p += (size_t)32 * nw * 8;
+  int *flag = reinterpret_cast<int *>(p);
+
+  // 1. scales
+  int bad = 0;
+  for (int i = t.tid; i < n; i += t.nt) scl[i] = pow2_scale(A[(size_t)i + (size_t)i * lda], bad);
+  t.sync();
+  // 2. stage As = S A S (FP32) with the row sums of |A| (ys as scratch), factor
+  float *rowabs = ys;
+  for (int i = t.tid; i < n; i += t.nt) rowabs[i] = 0.f;
+  t.sync();
+  team_load_panels<float, true>(t, L, A, lda, Ps, scl, rowabs);
+  t.sync();
+  float an_local = 0.f;
+  for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
+  const float an = team_max<float>(t, an_local, reinterpret_cast<float *>(red));
+  const double anorm = (double)an * (1.0 + 1e-6 * n);
+  const int fail = team_potrf_panel<float, true, true>(t, L, Ps, Ld, rinv,
+                                                      (float)n * 5.9604645e-08f, flag, true);
+  const int any_bad = team_any(t, bad, reinterpret_cast<int *>(red));
+  bool need_fb = fail != 0 || any_bad;
+  int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
+  const double tol_conv = 2.0 * sqrt((double)n) * PC_EPS64;
+  // 3. solve + refine, PC_MR right-hand sides at a time
+  for (int r0 = 0; r0 < m && !need_fb; r0 += PC_MR) {
+    const int nr = min(PC_MR, m - r0);
+    for (int q = 0; q < nr; q++) {
+      for (int i = t.tid; i < n; i += t.nt)
+        ys[q * n + i] = (float)B[(size_t)(r0 + q) + (size_t)i * ldb] * scl[i];
+      t.sync();
+      team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
+      for (int i = t.tid; i < n; i += t.nt) x[q * n + i] = (double)(ys[q * n + i] * scl[i]);
+      t.sync();
+    }
+    double bmax[PC_MR];
+    for (int q = 0; q < PC_MR; q++) {
+      double bm = 0.0;
+      if (q < nr)
+        for (int i = t.tid; i < n; i += t.nt) bm = fmax(bm, fabs(B[(size_t)(r0 + q) + (size_t)i * ldb]));
+      bmax[q] = team_max<double>(t, bm, red);
+    }
+    double eta_prev = INFINITY;
+    bool converged = false;
+    int step = 0;
+    for (;;) {
+      for (int q = 0; q < nr; q++)
+        team_residual_tiled(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n, colsum, true);
+      double eta = 0.0;
+      for (int q = 0; q < nr; q++) {
+        double rm = 0.0, xm = 0.0;
+        for (int i = t.tid; i < n; i += t.nt) {
+          rm = fmax(rm, fabs(r[q * n + i]));
+          xm = fmax(xm, fabs(x[q * n + i]));
+        }
+        // one reduction for both maxima: the residual is bounded by the
+        // product, so pack (rm, xm) as two lanes of the scratch
+        rm = team_max<double>(t, rm, red);
+        xm = team_max<double>(t, xm, red);
+        const double den = anorm * xm + bmax[q];
+        const double e = (den > 0.0) ? rm / den : (rm > 0.0 ? INFINITY : 0.0);
+        eta = (e > eta || e != e) ? e : eta;
+      }
+      if (eta <= tol_conv) {
+        converged = true;
+        break;
+      }
+      if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) break;
+      eta_prev = eta;
+      for (int q = 0; q < nr; q++) {
+        for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = (float)r[q * n + i] * scl[i];
+        t.sync();
+        team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
+        for (int i = t.tid; i < n; i += t.nt) x[q * n + i] += (double)(ys[q * n + i] * scl[i]);
+        t.sync();
+      }
+      step++;
+    }
+    steps_used = max(steps_used, step);
+    if (converged) {
+      for (int q = 0; q < nr; q++)
+        for (int i = t.tid; i < n; i += t.nt) B[(size_t)(r0 + q) + (size_t)i * ldb] = x[q * n + i];
+    } else {
+      need_fb = true;
+      fb_code = (step >= PC_ITMAX) ? -3 : -2;
+      fb_from = r0;
+    }
+    t.sync();
+  }
+  // 4. FP64 fallback
+  int info = 0;
+  if (need_fb)
+    info = panel_fp64_posv(t, n, m, fb_from, A, lda, B, ldb, Ps64_scratch, Ld64, rinv64, x, red,
+                           flag);
+  if (t.tid == 0) {
+    if (info_out) *info_out = need_fb ? info : 0;
+    if (iter_out) *iter_out = need_fb ? fb_code : steps_used;
+  }
+}
+
+// ===========================================================================
+// the persistent kernel
+// ===========================================================================
 template <bool MIXED>
-__global__ void __launch_bounds__(PC_NT)
+__global__ void __launch_bounds__(PC_NT, 1)
 posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int smem_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -366,57 +465,74 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
     const int TS = cfg.ts[c];
     const int team_id = threadIdx.x / TS;
     const int nteams = PC_NT / TS;
-    const size_t P = (size_t)n * (n + 1) / 2;
-    const bool lp_smem = (size_t)nteams * team_smem_bytes<MIXED>(n, TS, true) <= (size_t)smem_bytes;
-    const size_t tb = team_smem_bytes<MIXED>(n, TS, lp_smem);
-    const Team t{(int)(threadIdx.x % TS), TS, 1 + team_id};
+    const bool fac_smem = (size_t)nteams * team_smem_bytes<MIXED>(n, TS, true) <= (size_t)smem_bytes;
+    const size_t tb = team_smem_bytes<MIXED>(n, TS, fac_smem);
     const bool active = team_id < count;
-    // whole-warp teams without a system have nothing to synchronise with
-    if (active || TS < 32) {
-      long long sidx = 0;
-      int nn = n, m = 0, lda = 1, ldb = 1;
-      double *A = nullptr, *B = nullptr;
-      if (active) {
-        sidx = it.uniform ? (long long)start + team_id : (long long)it.perm[start + team_id];
-        sys.get(sidx, nn, m, A, lda, B, ldb);
-      }
-      unsigned char *base = smem + (size_t)team_id * tb;
-      // scratch slot: FP64 packed factors of all teams, then FP32 ones
-      double *Lp64_scratch = slot ? reinterpret_cast<double *>(slot) + (size_t)team_id * P : nullptr;
-      float *Lp32_scratch =
-          slot ? reinterpret_cast<float *>(reinterpret_cast<double *>(slot) + (size_t)nteams * P) +
-                     (size_t)team_id * P
-               : nullptr;
-      int *info_p = (active && out.info) ? out.info + sidx : nullptr;
-      int *iter_p = (active && out.iter) ? out.iter + sidx : nullptr;
-      if (MIXED) {
-        team_mixed_posv(t, active, n, m, A, lda, B, ldb, base, lp_smem, Lp32_scratch, Lp64_scratch,
-                        info_p, iter_p);
+    long long sidx = 0;
+    int m = 0, lda = 1, ldb = 1;
+    double *A = nullptr, *B = nullptr;
+    if (active) {
+      sidx = it.uniform ? (long long)start + team_id : (long long)it.perm[start + team_id];
+      sys.get(sidx, m, A, lda, B, ldb);
+    }
+    unsigned char *base = smem + (size_t)team_id * tb;
+    int *info_p = (active && out.info) ? out.info + sidx : nullptr;
+    int *iter_p = (active && out.iter) ? out.iter + sidx : nullptr;
+    if (n <= 32) {
+      // register path: every segment of each warp runs, idle ones on no data
+#define KGB_SMALL(WW)                                                                      \
+  if (MIXED) {                                                                             \
+    small_mixed_posv<WW>(active, n, m, A, lda, B, ldb, base, info_p, iter_p);              \
+  } else {                                                                                 \
+    double *ls_ = reinterpret_cast<double *>(base);                                        \
+    const int inf_ = small_fp64_posv<WW>(active, n, m, 0, A, lda, B, ldb, ls_,             \
+                                         ls_ + WW * (WW + 1));                             \
+    if (info_p && (threadIdx.x & (WW - 1)) == 0) *info_p = inf_;                           \
+  }
+      if (TS == 8) {
+        KGB_SMALL(8)
+      } else if (TS == 16) {
+        KGB_SMALL(16)
       } else {
-        double *Lp64 = lp_smem ? reinterpret_cast<double *>(base) : Lp64_scratch;
-        unsigned char *p = base + (lp_smem ? P * 8 : 0);
+        KGB_SMALL(32)
+      }
+#undef KGB_SMALL
+    } else if (active) {
+      const Team t{(int)(threadIdx.x % TS), TS, 1 + team_id};
+      const PanelLayout L = make_layout(n);
+      // scratch slot: FP64 panels of every team, then FP32 ones
+      double *P64s = slot ? reinterpret_cast<double *>(slot) + (size_t)team_id * L.total() : nullptr;
+      float *P32s = slot ? reinterpret_cast<float *>(reinterpret_cast<double *>(slot) +
+                                                       (size_t)nteams * L.total()) +
+                               (size_t)team_id * L.total()
+                         : nullptr;
+      if (MIXED) {
+        panel_mixed_posv(t, n, m, A, lda, B, ldb, base, fac_smem, P32s, P64s, info_p, iter_p);
+      } else {
+        double *Ps = fac_smem ? reinterpret_cast<double *>(base) : P64s;
+        unsigned char *p = base + (fac_smem ? L.total() * 8 : 0);
+        double *Ld = reinterpret_cast<double *>(p); p += 32 * LDD * 8;
         double *rinv = reinterpret_cast<double *>(p); p += (size_t)n * 8;
-        double *y = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
-        double *red = reinterpret_cast<double *>(p);
-        const int info = team_fp64_posv(t, active, n, m, 0, A, lda, B, ldb, Lp64, rinv, y, red);
-        if (info_p && t.tid == 0) *info_p = info;
+        double *y = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+        double *red = reinterpret_cast<double *>(p); p += (size_t)32 * (TS / 32) * 8;
+        int *flag = reinterpret_cast<int *>(p);
+        const int inf_ = panel_fp64_posv(t, n, m, 0, A, lda, B, ldb, Ps, Ld, rinv, y, red, flag);
+        if (info_p && t.tid == 0) *info_p = inf_;
       }
     }
     __syncthreads();
   }
 }
 
-// Bytes of global scratch each persistent CTA needs: the packed FP64 factors
-// of all teams of the largest item (mixed fallback / plain factors that do
-// not fit in shared memory).
+// Global scratch per CTA: FP64 + FP32 panel storage for every team of the
+// largest item (mixed fallback; factors that do not fit in shared memory).
 __host__ inline size_t posv_slot_bytes(const PosvCfg &cfg, int max_n) {
   size_t best = 0;
   for (int c = 0; c < PC_NCLS; c++) {
-    const int nhi = min(cfg.nmax[c], max_n);
     const int nlo = c ? cfg.nmax[c - 1] + 1 : 1;
-    if (nhi < nlo) continue;
-    const size_t P = (size_t)nhi * (nhi + 1) / 2;
-    const size_t b = (size_t)(PC_NT / cfg.ts[c]) * P * 12;  // FP64 + FP32 packed factors
+    const int nhi = min(cfg.nmax[c], max_n);
+    if (nhi < nlo || nhi <= 32) continue;
+    const size_t b = (size_t)(PC_NT / cfg.ts[c]) * make_layout(nhi).total() * 12;
     if (b > best) best = b;
   }
   return (best + 255) / 256 * 256;

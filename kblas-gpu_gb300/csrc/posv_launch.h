@@ -12,7 +12,7 @@
 namespace kgb {
 
 constexpr int PC_MAX_N = 1024;          // largest order the persistent kernels take
-constexpr size_t PC_SMEM_BUDGET = 200 * 1024;
+constexpr size_t PC_SMEM_BUDGET = 220 * 1024;
 
 struct PosvPlan {
   PosvCfg cfg;
@@ -47,13 +47,20 @@ static inline PosvCfg current_cfg(bool mixed) {
   return o.set[mixed ? 1 : 0] ? o.cfg[mixed ? 1 : 0] : default_cfg(mixed);
 }
 
+// A class whose orders are all <= 32 runs the register path: team size W in
+// {8, 16, 32} with W >= its largest order. A class with orders above 32 runs
+// the panel path: whole warps (32..256); one that straddles 32 needs W = 32.
 static inline bool cfg_valid(const PosvCfg &c) {
   for (int k = 0; k < PC_NCLS; k++) {
     const int ts = c.ts[k];
-    if (!(ts == 2 || ts == 4 || ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256))
-      return false;
+    const int nlo = k ? c.nmax[k - 1] + 1 : 1, nhi = c.nmax[k];
+    if (k && nhi <= c.nmax[k - 1]) return false;
+    if (!(ts == 8 || ts == 16 || ts == 32 || ts == 64 || ts == 128 || ts == 256)) return false;
     if (c.spi[k] < 1 || c.spi[k] * ts > PC_NT || (ts >= 64 && c.spi[k] > 15)) return false;
-    if (k && c.nmax[k] <= c.nmax[k - 1]) return false;
+    if (nlo <= 32 && ts < (nhi < 32 ? nhi : 32)) return false;  // W >= n on the register path
+    if (nlo <= 32 && nhi > 32 && ts != 32) return false;
+    if (nhi > 32 && ts < 32) return false;
+    if (ts < 32 && c.spi[k] * ts > PC_NT) return false;
   }
   return c.nmax[PC_NCLS - 1] >= PC_MAX_N;
 }

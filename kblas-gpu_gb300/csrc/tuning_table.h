@@ -5,10 +5,10 @@
 #pragma once
 
 // {nmax}, {team size}, {systems per item}
-#define KGB_TUNE_MIXED_NMAX {8, 16, 32, 64, 128, 512}
-#define KGB_TUNE_MIXED_TS {4, 4, 8, 32, 128, 256}
-#define KGB_TUNE_MIXED_SPI {64, 64, 32, 8, 2, 1}
+#define KGB_TUNE_MIXED_NMAX {8, 16, 32, 64, 128, 1024}
+#define KGB_TUNE_MIXED_TS {8, 16, 32, 32, 128, 256}
+#define KGB_TUNE_MIXED_SPI {32, 16, 8, 8, 2, 1}
 
-#define KGB_TUNE_PLAIN_NMAX {8, 16, 32, 64, 128, 512}
-#define KGB_TUNE_PLAIN_TS {4, 4, 8, 32, 128, 256}
-#define KGB_TUNE_PLAIN_SPI {64, 64, 32, 8, 2, 1}
+#define KGB_TUNE_PLAIN_NMAX {8, 16, 32, 64, 128, 1024}
+#define KGB_TUNE_PLAIN_TS {8, 16, 32, 32, 128, 256}
+#define KGB_TUNE_PLAIN_SPI {32, 16, 8, 8, 2, 1}
