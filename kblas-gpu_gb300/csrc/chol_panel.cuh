@@ -84,6 +84,45 @@ __device__ __forceinline__ int warp_chol_rot(T (&v)[32], int jb, T tol, T *Lrow,
   return fail;
 }
 
+// Warp-level inverse of the factored diagonal block: lane j computes column j
+// of X = L_JJ^{-1} by forward substitution (X[k] = 0 above the diagonal) from
+// the row-major copy Ld; X goes to the lower part of the panel's diagonal
+// square and X^T to its strict upper part.
+template <typename T>
+__device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T *Ld, const T *rinvJ)
+{
+  const int lane = threadIdx.x & 31;
+      // lane j: column j of X = L_JJ^{-1} by forward substitution (X[k] = 0
+      // above the diagonal); X -> lower part, X^T -> strict upper part
+      T X[32];
+#pragma unroll
+      for (int k = 0; k < 32; k++) X[k] = T(0);
+      for (int i = 0; i < jb; i++) {
+        T s0 = (i == lane) ? T(1) : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        const T *li = Ld + i * LDD;
+#pragma unroll
+        for (int k = 0; k < 32; k += 4) {
+          if (k < i) s0 -= li[k] * X[k];
+          if (k + 1 < i) s1 -= li[k + 1] * X[k + 1];
+          if (k + 2 < i) s2 -= li[k + 2] * X[k + 2];
+          if (k + 3 < i) s3 -= li[k + 3] * X[k + 3];
+        }
+        const T xi = ((s0 + s1) + (s2 + s3)) * rinvJ[i];
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+          if (k == i) X[k] = xi;
+      }
+      if (lane < jb) {
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+          if (k < jb) {
+            if (k >= lane) Pp[k + lane * ld] = X[k];
+            if (k > lane) Pp[lane + k * ld] = X[k];
+          }
+        }
+      }
+}
+
 // ----------------------------------------------------------------------------
 // Panel Cholesky of the team's matrix. Ps: panel storage (shared or global).
 // Ld: 32 x 32 row-major scratch (shared) for the current diagonal block.
@@ -110,40 +149,10 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
       for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
       const int f = warp_chol_rot<T, 32, CHECK_INF>(v, jb, tol, Ld, LDD, rinv + J);
       __syncwarp();
-      if (!INV) {
-        // write L_JJ back column by column (coalesced in the panel)
-        for (int c = 0; c < jb; c++)
-          if (lane >= c && lane < jb) Pp[lane + c * ld] = Ld[lane * LDD + c];
-      } else {
-        // lane j computes column j of X = L_JJ^{-1} by forward substitution
-        // (X[k] = 0 above the diagonal), then X goes to the lower part and
-        // X^T to the strict upper part of the diagonal square
-        T X[32];
-#pragma unroll
-        for (int k = 0; k < 32; k++) X[k] = T(0);
-        for (int i = 0; i < jb; i++) {
-          T s = (i == lane) ? T(1) : T(0);
-          const T *li = Ld + i * LDD;
-#pragma unroll
-          for (int k = 0; k < 32; k++)
-            if (k < i) s -= li[k] * X[k];
-          const T xi = s * rinv[J + i];
-#pragma unroll
-          for (int k = 0; k < 32; k++)
-            if (k == i) X[k] = xi;
-        }
-        __syncwarp();
-        if (lane < jb) {
-#pragma unroll
-          for (int k = 0; k < 32; k++) {
-            if (k < jb) {
-              // X[k] = Xinv(k, lane): lower entry (k, lane) and mirrored (lane, k)
-              if (k >= lane) Pp[k + lane * ld] = X[k];
-              if (k > lane) Pp[lane + k * ld] = X[k];
-            }
-          }
-        }
-      }
+      // write L_JJ back column by column (coalesced in the panel); with INV it
+      // is replaced by the inverse later in this step
+      for (int c = 0; c < jb; c++)
+        if (lane >= c && lane < jb) Pp[lane + c * ld] = Ld[lane * LDD + c];
       if (lane == 0) *flag = f ? J + f : 0;
     }
     t.sync();
@@ -176,8 +185,14 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
         if (c < jb) Pp[i + c * ld] = x[c];
     }
     t.sync();
-    // (c) trailing update of every later panel with this one, 4 x 4 tiles
-    {
+    // (c) trailing update of every later panel with this one, 4 x 4 tiles;
+    // with INV, warp 0 meanwhile turns L_JJ into its inverse (it is not read
+    // by the update, which only uses the rows below the diagonal block)
+    const bool ovl = INV && t.nt >= 64;  // a spare warp inverts during the update
+    if (ovl && w == 0) {
+      warp_invert_diag<T>(Pp, ld, jb, Ld, rinv + J);
+    } else {
+      const int utid = ovl ? t.tid - 32 : t.tid, unt = ovl ? t.nt - 32 : t.nt;
       // count tiles per later panel: row tiles ceil(mq/4) x col tiles jbq/4 (jbq rounded up)
       int tile0 = 0;
       for (int q = p + 1; q < L.np; q++) {
@@ -186,8 +201,8 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
         const int ntile = rt * ct;
         T *Pq = Ps + L.base(q);
         const int ldq = L.ldp(q);
-        const int start = ((t.tid - tile0) % t.nt + t.nt) % t.nt;
-        for (int tt = start; tt < ntile; tt += t.nt) {
+        const int start = ((utid - tile0) % unt + unt) % unt;
+        for (int tt = start; tt < ntile; tt += unt) {
           const int c4 = tt / rt, r4 = tt - c4 * rt;
           const int i0 = r4 * 4, c0 = c4 * 4;  // rows K+i0.., cols c0.. of panel q
           if (i0 + 3 < c0) continue;           // entirely above the diagonal
@@ -231,6 +246,10 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
       }
     }
     t.sync();
+    if (INV && !ovl) {
+      warp_invert_diag<T>(Pp, ld, jb, Ld, rinv + J);
+      t.sync();
+    }
   }
   (void)lane;
   (void)nw;
@@ -378,7 +397,8 @@ __device__ void team_llt_solve_panel(const Team &t, const PanelLayout &L, const 
 // of type T. SCALE: FP32 value (float)a_ij * scl[i] * scl[j]. Padding rows and
 // the strict upper part of each diagonal block are zeroed.
 // Stage the lower triangle of A (FP64, column-major, lda) into panel storage
-// of type T (SCALE: FP32 (float)a_ij * scl[i] * scl[j]). One thread per panel
+// of type T (SCALE: FP32 a_ij * 2^(sh[i] + sh[j]), converted on the integer
+// pipe, see f64_to_f32_scaled; sh = -e of the row scale 2^-e). One thread per panel
 // row issues the 32 loads of the row before using any (32 loads in flight).
 // Padding rows and the strict upper part of each diagonal block get zeros.
 // rowabs (may be NULL): rowabs[i] += sum_j |a_ij| over the whole symmetric
@@ -386,7 +406,7 @@ __device__ void team_llt_solve_panel(const Team &t, const PanelLayout &L, const 
 // mirrored column part by a warp transpose-sum), for ||A||_inf.
 template <typename T, bool SCALE>
 __device__ void team_load_panels(const Team &t, const PanelLayout &L, const double *__restrict__ A,
-                                 int lda, T *Ps, const float *scl, float *rowabs)
+                                 int lda, T *Ps, const int *sh, float *rowabs)
 {
   const int lane = t.lane();
   for (int p = 0; p < L.np; p++) {
@@ -397,22 +417,22 @@ __device__ void team_load_panels(const Team &t, const PanelLayout &L, const doub
       const int i = J + ii;
       const bool in = ii < ld;        // a row of the panel (padding rows get zeros)
       const bool real = i < L.n;      // a row of the matrix
-      const float si = (SCALE && real) ? scl[i] : 1.0f;
+      const int si = (SCALE && real) ? sh[i] : 0;
       float rsum = 0.f;
+      double a[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        a[c] = (real && c < jb && ii >= c) ? A[(size_t)i + (size_t)(J + c) * lda] : 0.0;
 #pragma unroll
       for (int h = 0; h < 32; h += 16) {
-        double a[16];
-#pragma unroll
-        for (int c = 0; c < 16; c++)
-          a[c] = (real && h + c < jb && ii >= h + c) ? A[(size_t)i + (size_t)(J + h + c) * lda] : 0.0;
         float cabs[16];
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-          const float af = (float)a[c];
+          const float af = f64_to_f32_scaled(a[h + c], 0);
           if (in && h + c < jb) {
             T v;
-            if (SCALE) v = (T)(af * si * scl[J + h + c]);
-            else v = (T)a[c];
+            if (SCALE) v = (T)f64_to_f32_scaled(a[h + c], si + sh[J + h + c]);
+            else v = (T)a[h + c];
             Pp[ii + (h + c) * ld] = v;
           }
           rsum += fabsf(af);

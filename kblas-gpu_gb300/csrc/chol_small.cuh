@@ -13,7 +13,7 @@ namespace kgb {
 // the power-of-two scaling of the mixed path, or plain. Loads of one column
 // are coalesced across the lanes.
 template <typename T, int W, bool SCALE>
-__device__ __forceinline__ void small_load(int n, const double *A, int lda, float sc_lane,
+__device__ __forceinline__ void small_load(int n, const double *A, int lda, int sh_lane,
                                            bool active, T (&v)[32])
 {
   const int lane = threadIdx.x & (W - 1);
@@ -24,8 +24,8 @@ __device__ __forceinline__ void small_load(int n, const double *A, int lda, floa
 #pragma unroll
   for (int c = 0; c < 32; c++) {
     if (c < W) {
-      const float sc_c = __shfl_sync(0xffffffffu, sc_lane, c, W);
-      v[c] = SCALE ? (T)((float)a[c] * sc_lane * sc_c) : (T)a[c];
+      const int sh_c = __shfl_sync(0xffffffffu, sh_lane, c, W);
+      v[c] = SCALE ? (T)f64_to_f32_scaled(a[c], sh_lane + sh_c) : (T)a[c];
     } else {
       v[c] = T(0);
     }

@@ -49,6 +49,25 @@ __device__ __forceinline__ void tri_advance(int &ii, int &kk, int step) {
   }
 }
 
+// FP64 -> FP32 conversion with a power-of-two scale 2^k applied exactly,
+// done on the IEEE-754 bit patterns with integer operations only (the
+// hardware conversion shares the scarce FP64 pipe on this part). Rounds to
+// nearest (ties away from zero), flushes results below the FP32 normal range
+// to signed zero and returns signed infinity above it; a NaN input gives NaN.
+__device__ __forceinline__ float f64_to_f32_scaled(double a, int k) {
+  const unsigned hi = (unsigned)__double2hiint(a);
+  const unsigned lo = (unsigned)__double2loint(a);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FF);
+  if (e == 0x7FF) return __int_as_float((int)(sign | 0x7F800000u | ((hi & 0xFFFFFu) | lo ? 0x400000u : 0u)));
+  const int fe = e - 1023 + 127 + k;
+  if (e == 0 || fe <= 0) return __int_as_float((int)sign);
+  if (fe >= 255) return __int_as_float((int)(sign | 0x7F800000u));
+  unsigned bits = ((unsigned)fe << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  bits += (lo >> 28) & 1u;  // carry into the exponent is the correct rounding
+  return __int_as_float((int)(sign | bits));
+}
+
 template <typename T>
 __device__ __forceinline__ bool is_pos_pivot(T d) {
   return d > T(0);  // false for NaN

@@ -117,7 +117,7 @@ __host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool f
   b += 32 * LDD * 8;                               // diagonal block (FP64 size: fallback too)
   b += (size_t)n * 8;                              // rinv (FP64 size: fallback too)
   if (MIXED) {
-    b += (size_t)n * 4;                            // scales
+    b += (size_t)n * 8;                            // scales + exponent shifts
     b += (size_t)PC_MR * n * 4;                    // FP32 solve vectors
     b = (b + 7) / 8 * 8;
     b += 2 * (size_t)PC_MR * n * 8;                // x, r
@@ -146,8 +146,10 @@ __device__ __forceinline__ int seg_any(int v, int W) {
   return ((ball >> base) & ((1u << W) - 1u)) != 0u;
 }
 
-// power-of-two scale of row i from the FP64 diagonal; bad = outside FP32 range
-__device__ __forceinline__ float pow2_scale(double d, int &bad) {
+// power-of-two scale 2^sh of row i from the FP64 diagonal (sh = -floor(
+// log2(a_ii) / 2)); bad = outside the FP32 range
+__device__ __forceinline__ float pow2_scale(double d, int &bad, int &sh) {
+  sh = 0;
   if (d > 0.0 && d < 1e300) {
     int e = ilogb(d);
     e = (e >= 0) ? e / 2 : -((-e + 1) / 2);  // floor(log2(d) / 2)
@@ -155,6 +157,7 @@ __device__ __forceinline__ float pow2_scale(double d, int &bad) {
       bad = 1;
       return 1.0f;
     }
+    sh = -e;
     return ldexpf(1.0f, -e);
   }
   bad = 1;  // non-positive / NaN / huge diagonal: the FP64 path decides
@@ -173,7 +176,7 @@ __device__ int small_fp64_posv(bool active, int n, int m, int r_from, double *A,
 {
   const int lane = threadIdx.x & (W - 1);
   double v[32];
-  small_load<double, W, false>(n, active ? A : nullptr, lda, 1.0f, active, v);
+  small_load<double, W, false>(n, active ? A : nullptr, lda, 0, active, v);
   const int fail = warp_chol_rot<double, W, false>(v, n, 0.0, Ls64, W + 1, rinv64);
   __syncwarp();
   if (active && lane < n) {
@@ -202,12 +205,12 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
   float *Ls = reinterpret_cast<float *>(rinv64 + W);
   float *rinv = Ls + W * (W + 1);
   float *scl = rinv + W;
-  int bad = 0;
+  int bad = 0, shl = 0;
   float sc = 1.0f;
-  if (active && lane < n) sc = pow2_scale(A[(size_t)lane + (size_t)lane * lda], bad);
+  if (active && lane < n) sc = pow2_scale(A[(size_t)lane + (size_t)lane * lda], bad, shl);
   scl[lane] = sc;
   float v[32];
-  small_load<float, W, true>(n, active ? A : nullptr, lda, sc, active, v);
+  small_load<float, W, true>(n, active ? A : nullptr, lda, shl, active, v);
   // ||A||_inf from the staged values (|a_ij| = |as_ij| / (s_i s_j), exact)
 #pragma unroll
   for (int c = 0; c < W; c++)
@@ -231,7 +234,7 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
   for (int r0 = 0; r0 < m_hi; r0++) {
     const bool go = active && !need_fb && r0 < m;
     const double b = (go && lane < n) ? B[(size_t)r0 + (size_t)lane * ldb] : 0.0;
-    float y = small_llt_solve<float, W>(n, Ls, rinv, (float)b * sc);
+    float y = small_llt_solve<float, W>(n, Ls, rinv, f64_to_f32_scaled(b, shl));
     double x = (double)(y * sc);
     double eta_prev = INFINITY;
     bool going = go, converged = false;
@@ -253,7 +256,7 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
           eta_prev = eta;
         }
       }
-      y = small_llt_solve<float, W>(n, Ls, rinv, going ? (float)r * sc : 0.0f);
+      y = small_llt_solve<float, W>(n, Ls, rinv, going ? f64_to_f32_scaled(r, shl) : 0.0f);
       if (going) {
         x += (double)(y * sc);
         step++;
@@ -321,6 +324,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   double *rinv64 = reinterpret_cast<double *>(p); p += (size_t)n * 8;
   float *rinv = reinterpret_cast<float *>(rinv64);
   float *scl = reinterpret_cast<float *>(p); p += (size_t)n * 4;
+  int *sh = reinterpret_cast<int *>(p); p += (size_t)n * 4;
   float *ys = reinterpret_cast<float *>(p); p += (size_t)PC_MR * n * 4;
   p = reinterpret_cast<unsigned char *>(((uintptr_t)p + 7) & ~(uintptr_t)7);
   double *x = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
@@ -331,13 +335,17 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
 
   // 1. scales
   int bad = 0;
-  for (int i = t.tid; i < n; i += t.nt) scl[i] = pow2_scale(A[(size_t)i + (size_t)i * lda], bad);
+  for (int i = t.tid; i < n; i += t.nt) {
+    int e;
+    scl[i] = pow2_scale(A[(size_t)i + (size_t)i * lda], bad, e);
+    sh[i] = e;
+  }
   t.sync();
   // 2. stage As = S A S (FP32) with the row sums of |A| (ys as scratch), factor
   float *rowabs = ys;
   for (int i = t.tid; i < n; i += t.nt) rowabs[i] = 0.f;
   t.sync();
-  team_load_panels<float, true>(t, L, A, lda, Ps, scl, rowabs);
+  team_load_panels<float, true>(t, L, A, lda, Ps, sh, rowabs);
   t.sync();
   float an_local = 0.f;
   for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
@@ -354,7 +362,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
     const int nr = min(PC_MR, m - r0);
     for (int q = 0; q < nr; q++) {
       for (int i = t.tid; i < n; i += t.nt)
-        ys[q * n + i] = (float)B[(size_t)(r0 + q) + (size_t)i * ldb] * scl[i];
+        ys[q * n + i] = f64_to_f32_scaled(B[(size_t)(r0 + q) + (size_t)i * ldb], sh[i]);
       t.sync();
       team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
       for (int i = t.tid; i < n; i += t.nt) x[q * n + i] = (double)(ys[q * n + i] * scl[i]);
@@ -395,7 +403,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
       if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) break;
       eta_prev = eta;
       for (int q = 0; q < nr; q++) {
-        for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = (float)r[q * n + i] * scl[i];
+        for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = f64_to_f32_scaled(r[q * n + i], sh[i]);
         t.sync();
         team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
         for (int i = t.tid; i < n; i += t.nt) x[q * n + i] += (double)(ys[q * n + i] * scl[i]);
@@ -428,6 +436,41 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
 // ===========================================================================
 // the persistent kernel
 // ===========================================================================
+
+__device__ __forceinline__ void item_decode(const ItemArgs &it, const PosvCfg &cfg, long long q,
+                                            int &n, int &start, int &count) {
+  if (it.uniform) {
+    n = it.n_uniform;
+    const int spi = cfg.spi[pc_class(cfg, n)];
+    start = (int)(q * spi);
+    count = (int)min((long long)spi, it.batch - q * spi);
+  } else {
+    const int4 e = it.items[q];
+    n = e.x;
+    start = e.y;
+    count = e.z;
+  }
+}
+
+// Ask L2 for the lower triangles of the next item's matrices while the
+// current item is being processed (one prefetch per 128-byte line), so the
+// next item's staging loads hit L2 instead of waiting on HBM.
+__device__ __forceinline__ void prefetch_item(const SysArgs &sys, const ItemArgs &it,
+                                              const PosvCfg &cfg, long long q) {
+  int n, start, count;
+  item_decode(it, cfg, q, n, start, count);
+  const int pairs = count * n;  // (system, column) pairs
+  for (int pc = threadIdx.x; pc < pairs; pc += blockDim.x) {
+    const int k = pc / n, j = pc - k * n;
+    const long long sidx = it.uniform ? (long long)start + k : (long long)it.perm[start + k];
+    int m, lda, ldb;
+    double *A, *B;
+    sys.get(sidx, m, A, lda, B, ldb);
+    const char *lo = reinterpret_cast<const char *>(A + (size_t)j + (size_t)j * lda);
+    const char *hi = reinterpret_cast<const char *>(A + (size_t)n + (size_t)j * lda);
+    for (const char *a = lo; a < hi; a += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+  }
+}
 template <bool MIXED>
 __global__ void __launch_bounds__(PC_NT, 1)
 posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int smem_bytes)
@@ -443,24 +486,18 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
   }
   char *slot = out.scratch ? out.scratch + (size_t)blockIdx.x * out.slot_bytes : nullptr;
 
+  if (threadIdx.x == 0) s_item = atomicAdd(it.queue, 1);
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(it.queue, 1);
     __syncthreads();
     const long long q = s_item;
     __syncthreads();
     if (q >= nitems) break;
+    // claim the next item now and warm L2 with its matrices
+    if (threadIdx.x == 0) s_item = atomicAdd(it.queue, 1);
+    __syncthreads();
+    if (s_item < nitems) prefetch_item(sys, it, cfg, s_item);
     int n, start, count;
-    if (it.uniform) {
-      n = it.n_uniform;
-      const int spi = cfg.spi[pc_class(cfg, n)];
-      start = (int)(q * spi);
-      count = (int)min((long long)spi, it.batch - q * spi);
-    } else {
-      const int4 e = it.items[q];
-      n = e.x;
-      start = e.y;
-      count = e.z;
-    }
+    item_decode(it, cfg, q, n, start, count);
     const int c = pc_class(cfg, n);
     const int TS = cfg.ts[c];
     const int team_id = threadIdx.x / TS;
