@@ -94,13 +94,16 @@ class VWorkload:
                     a = g @ g.transpose(1, 2)
                     a.diagonal(dim1=1, dim2=2).add_(float(n))
                     if grp:
-                        w_, v_ = torch.linalg.eigh(a)
-                        k = torch.randint(0, n, (len(s_),), generator=gen, device=dev)
-                        ar = torch.arange(len(s_), device=dev)
+                        # flip one eigenvalue (numpy on the host: ~1% of the batch)
+                        an = a.cpu().numpy()
+                        w_, v_ = np.linalg.eigh(an)
+                        k = torch.randint(0, n, (len(s_),), generator=gen, device=dev).cpu().numpy()
+                        ar = np.arange(len(s_))
                         vk = v_[ar, :, k]
                         wk = w_[ar, k]
-                        a = a - 2.0 * wk[:, None, None] * vk[:, :, None] * vk[:, None, :]
-                        a = 0.5 * (a + a.transpose(1, 2))
+                        an = an - 2.0 * wk[:, None, None] * vk[:, :, None] * vk[:, None, :]
+                        an = 0.5 * (an + an.transpose(0, 2, 1))
+                        a = torch.from_numpy(an).to(dev)
                     o0 = int(offs[s_[0]])
                     self.A[o0:o0 + len(s_) * n * n].copy_(a.reshape(-1))  # symmetric: col-major == row-major
                     del g, a

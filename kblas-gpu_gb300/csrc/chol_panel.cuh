@@ -84,43 +84,43 @@ __device__ __forceinline__ int warp_chol_rot(T (&v)[32], int jb, T tol, T *Lrow,
   return fail;
 }
 
-// Warp-level inverse of the factored diagonal block: lane j computes column j
-// of X = L_JJ^{-1} by forward substitution (X[k] = 0 above the diagonal) from
-// the row-major copy Ld; X goes to the lower part of the panel's diagonal
-// square and X^T to its strict upper part.
+// Warp-level inverse of a factored diagonal block held in the panel's
+// diagonal square (lower part, column-major, leading dimension ld): lane j
+// computes column j of X = L^{-1} by forward substitution (X[k] = 0 above the
+// diagonal), reading L with broadcast loads; then X replaces L in the lower
+// part and X^T fills the strict upper part.
 template <typename T>
-__device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T *Ld, const T *rinvJ)
+__device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T *rinvJ)
 {
   const int lane = threadIdx.x & 31;
-      // lane j: column j of X = L_JJ^{-1} by forward substitution (X[k] = 0
-      // above the diagonal); X -> lower part, X^T -> strict upper part
-      T X[32];
+  T X[32];
 #pragma unroll
-      for (int k = 0; k < 32; k++) X[k] = T(0);
-      for (int i = 0; i < jb; i++) {
-        T s0 = (i == lane) ? T(1) : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-        const T *li = Ld + i * LDD;
+  for (int k = 0; k < 32; k++) X[k] = T(0);
+  for (int i = 0; i < jb; i++) {
+    T s0 = (i == lane) ? T(1) : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
 #pragma unroll
-        for (int k = 0; k < 32; k += 4) {
-          if (k < i) s0 -= li[k] * X[k];
-          if (k + 1 < i) s1 -= li[k + 1] * X[k + 1];
-          if (k + 2 < i) s2 -= li[k + 2] * X[k + 2];
-          if (k + 3 < i) s3 -= li[k + 3] * X[k + 3];
-        }
-        const T xi = ((s0 + s1) + (s2 + s3)) * rinvJ[i];
+    for (int k = 0; k < 32; k += 4) {
+      if (k < i) s0 -= Pp[i + k * ld] * X[k];
+      if (k + 1 < i) s1 -= Pp[i + (k + 1) * ld] * X[k + 1];
+      if (k + 2 < i) s2 -= Pp[i + (k + 2) * ld] * X[k + 2];
+      if (k + 3 < i) s3 -= Pp[i + (k + 3) * ld] * X[k + 3];
+    }
+    const T xi = ((s0 + s1) + (s2 + s3)) * rinvJ[i];
 #pragma unroll
-        for (int k = 0; k < 32; k++)
-          if (k == i) X[k] = xi;
+    for (int k = 0; k < 32; k++)
+      if (k == i) X[k] = xi;
+  }
+  __syncwarp();
+  if (lane < jb) {
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      if (k < jb) {
+        if (k >= lane) Pp[k + lane * ld] = X[k];
+        if (k > lane) Pp[lane + k * ld] = X[k];
       }
-      if (lane < jb) {
-#pragma unroll
-        for (int k = 0; k < 32; k++) {
-          if (k < jb) {
-            if (k >= lane) Pp[k + lane * ld] = X[k];
-            if (k > lane) Pp[lane + k * ld] = X[k];
-          }
-        }
-      }
+    }
+  }
+  __syncwarp();
 }
 
 // ----------------------------------------------------------------------------
@@ -188,11 +188,8 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
     // (c) trailing update of every later panel with this one, 4 x 4 tiles;
     // with INV, warp 0 meanwhile turns L_JJ into its inverse (it is not read
     // by the update, which only uses the rows below the diagonal block)
-    const bool ovl = INV && t.nt >= 64;  // a spare warp inverts during the update
-    if (ovl && w == 0) {
-      warp_invert_diag<T>(Pp, ld, jb, Ld, rinv + J);
-    } else {
-      const int utid = ovl ? t.tid - 32 : t.tid, unt = ovl ? t.nt - 32 : t.nt;
+    {
+      const int utid = t.tid, unt = t.nt;
       // count tiles per later panel: row tiles ceil(mq/4) x col tiles jbq/4 (jbq rounded up)
       int tile0 = 0;
       for (int q = p + 1; q < L.np; q++) {
@@ -246,13 +243,167 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
       }
     }
     t.sync();
-    if (INV && !ovl) {
-      warp_invert_diag<T>(Pp, ld, jb, Ld, rinv + J);
-      t.sync();
-    }
+  }
+  if (INV && !fail) {
+    // the diagonal blocks are independent now: each warp inverts its share
+    for (int p = w; p < L.np; p += nw) warp_invert_diag<T>(Ps + L.base(p), L.ldp(p), L.jb(p), rinv + p * PNB);
+    t.sync();
   }
   (void)lane;
-  (void)nw;
+  return fail;
+}
+
+// ----------------------------------------------------------------------------
+// One 4 x 4 tile of the trailing update C -= P P^T: rows K+i0.., columns
+// c0.. of the later panel q (Pq, ldq, jq columns) from rows of panel p.
+template <typename T>
+__device__ __forceinline__ void panel_tile_update(const T *Pp, int ld, int jb, int KmJ, int i0,
+                                                  int c0, T *Pq, int ldq, int jq)
+{
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+  const T *arow = Pp + KmJ + i0;
+  const T *brow = Pp + KmJ + c0;
+  for (int k = 0; k < jb; k++) {
+    T a[4], b[4];
+    if (sizeof(T) == 4) {
+      const float4 av = *reinterpret_cast<const float4 *>(arow + (size_t)k * ld);
+      const float4 bv = *reinterpret_cast<const float4 *>(brow + (size_t)k * ld);
+      a[0] = av.x; a[1] = av.y; a[2] = av.z; a[3] = av.w;
+      b[0] = bv.x; b[1] = bv.y; b[2] = bv.z; b[3] = bv.w;
+    } else {
+      const double2 a01 = *reinterpret_cast<const double2 *>(arow + (size_t)k * ld);
+      const double2 a23 = *reinterpret_cast<const double2 *>(arow + (size_t)k * ld + 2);
+      const double2 b01 = *reinterpret_cast<const double2 *>(brow + (size_t)k * ld);
+      const double2 b23 = *reinterpret_cast<const double2 *>(brow + (size_t)k * ld + 2);
+      a[0] = a01.x; a[1] = a01.y; a[2] = a23.x; a[3] = a23.y;
+      b[0] = b01.x; b[1] = b01.y; b[2] = b23.x; b[3] = b23.y;
+    }
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++) acc[x][y] += a[x] * b[y];
+  }
+#pragma unroll
+  for (int y = 0; y < 4; y++) {
+    if (c0 + y < jq) {
+      T *col = Pq + (size_t)(c0 + y) * ldq + i0;
+#pragma unroll
+      for (int x = 0; x < 4; x++) col[x] -= acc[x][y];  // padding rows absorb the overhang
+    }
+  }
+}
+
+// Warp 0: factor the diagonal block of panel p in registers; L -> panel and
+// -> Ldb (row-major copy, stride LDD); 1/L(c,c) -> rinv; *flag = failing
+// column (global, 1-based) or 0.
+template <typename T, bool CHECK_INF>
+__device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T *Ps, T *Ldb, T *rinv,
+                                                 T tol, int *flag)
+{
+  const int lane = threadIdx.x & 31;
+  const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+  T *Pp = Ps + L.base(p);
+  T v[32];
+#pragma unroll
+  for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
+  const int f = warp_chol_rot<T, 32, CHECK_INF>(v, jb, tol, Ldb, LDD, rinv + J);
+  __syncwarp();
+  for (int c = 0; c < jb; c++)
+    if (lane >= c && lane < jb) Pp[lane + c * ld] = Ldb[lane * LDD + c];
+  if (lane == 0) *flag = f ? J + f : 0;
+  __syncwarp();
+}
+
+// Panel Cholesky with look-ahead, for teams of at least two warps: while
+// warps 1.. apply the trailing update of step p, warp 0 updates the next
+// diagonal block first and factors it, so the 32-step dependent chain of each
+// diagonal factorization overlaps the bulk update instead of stalling the
+// team. Ld2 holds two row-major 32 x LDD copies (current and next block).
+// INV: afterwards every diagonal square is replaced by its inverse (lower)
+// and the transpose of the inverse (strict upper), one block per warp.
+template <typename T, bool CHECK_INF, bool INV>
+__device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T *Ld2, T *rinv,
+                                   T tol, int *flag)
+{
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  if (w == 0) warp_factor_diag<T, CHECK_INF>(L, 0, Ps, Ld2, rinv, tol, flag);
+  t.sync();
+  int fail = *flag;
+  for (int p = 0; p < L.np && !fail; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    T *Pp = Ps + L.base(p);
+    const T *Ld = Ld2 + (p & 1) * 32 * LDD;
+    // (b) rows below the diagonal block: x * L_JJ^T = p
+    const int rows = L.n - J;
+    for (int i = jb + t.tid; i < rows; i += t.nt) {
+      T x[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) x[c] = (c < jb) ? Pp[i + c * ld] : T(0);
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        if (c < jb) {
+          T s0 = x[c], s1 = T(0);
+          const T *lrow = Ld + c * LDD;
+#pragma unroll
+          for (int q = 0; q < 32; q++) {
+            if (q < c) {
+              if (q & 1) s1 -= x[q] * lrow[q];
+              else s0 -= x[q] * lrow[q];
+            }
+          }
+          x[c] = (s0 + s1) * rinv[J + c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < jb) Pp[i + c * ld] = x[c];
+    }
+    t.sync();
+    // (c) trailing update; warp 0 takes the next diagonal block first
+    if (w == 0) {
+      if (p + 1 < L.np) {
+        const int q = p + 1, K = q * PNB, mq = L.n - K, jq = L.jb(q);
+        const int rt = min((mq + 3) >> 2, 8), ct = (jq + 3) >> 2;
+        T *Pq = Ps + L.base(q);
+        for (int tt = lane; tt < rt * ct; tt += 32) {
+          const int c4 = tt / rt, r4 = tt - c4 * rt;
+          if (r4 * 4 + 3 < c4 * 4) continue;
+          panel_tile_update<T>(Pp, ld, jb, K - J, r4 * 4, c4 * 4, Pq, L.ldp(q), jq);
+        }
+        __syncwarp();
+        warp_factor_diag<T, CHECK_INF>(L, q, Ps, Ld2 + (q & 1) * 32 * LDD, rinv, tol, flag);
+      }
+    } else {
+      const int utid = t.tid - 32, unt = t.nt - 32;
+      int tile0 = 0;
+      for (int q = p + 1; q < L.np; q++) {
+        const int K = q * PNB, mq = L.n - K, jq = L.jb(q);
+        const int rt = (mq + 3) >> 2, ct = (jq + 3) >> 2;
+        const int ntile = rt * ct;
+        T *Pq = Ps + L.base(q);
+        const int ldq = L.ldp(q);
+        const int start = ((utid - tile0) % unt + unt) % unt;
+        for (int tt = start; tt < ntile; tt += unt) {
+          const int c4 = tt / rt, r4 = tt - c4 * rt;
+          if (q == p + 1 && r4 < 8) continue;  // the next diagonal block: warp 0
+          if (r4 * 4 + 3 < c4 * 4) continue;
+          panel_tile_update<T>(Pp, ld, jb, K - J, r4 * 4, c4 * 4, Pq, ldq, jq);
+        }
+        tile0 += ntile;
+      }
+    }
+    t.sync();
+    fail = *flag;
+  }
+  if (INV && !fail) {
+    for (int p = w; p < L.np; p += nw) warp_invert_diag<T>(Ps + L.base(p), L.ldp(p), L.jb(p), rinv + p * PNB);
+    t.sync();
+  }
+  (void)lane;
   return fail;
 }
 

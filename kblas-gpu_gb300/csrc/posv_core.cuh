@@ -351,8 +351,10 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
   const float an = team_max<float>(t, an_local, reinterpret_cast<float *>(red));
   const double anorm = (double)an * (1.0 + 1e-6 * n);
-  const int fail = team_potrf_panel<float, true, true>(t, L, Ps, Ld, rinv,
-                                                      (float)n * 5.9604645e-08f, flag, true);
+  const float ftol = (float)n * 5.9604645e-08f;  // n * 2^-24
+  const int fail = (t.nt >= 64)
+                       ? team_potrf_panel_la<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag)
+                       : team_potrf_panel<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag, true);
   const int any_bad = team_any(t, bad, reinterpret_cast<int *>(red));
   bool need_fb = fail != 0 || any_bad;
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
