@@ -25,6 +25,7 @@
 #ifndef KBLAS_GB300_BATCH_H
 #define KBLAS_GB300_BATCH_H
 
+#include <cuda_runtime_api.h>
 #include "kblas_defs.h"
 
 #ifdef __cplusplus
@@ -207,6 +208,26 @@ int kblasDposv_vbatch_mixed(kblasHandle_t handle, char side, char uplo,
  * two) and the systems per work item. Six entries each; NULL restores the
  * table compiled into the library. Used by the committed autotuner. */
 int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi);
+
+/* Allocation-free mixed-precision POSV (no counterpart in the reference).
+ * Same arguments, semantics and results as kblasDposv_batch_mixed_strided,
+ * but it takes a CUDA stream instead of a handle and allocates nothing: its
+ * scratch is one fixed array per device in the library's device image. For
+ * callers that cannot allocate when they solve (a framework that owns all
+ * device memory, a latency-bound loop where cudaMalloc / cudaFree would stall
+ * or fail). Limits: n <= KBLAS_POSV_NOALLOC_MAX_N, else a message and
+ * KBLAS_NotSupported; scratch KBLAS_POSV_NOALLOC_SCRATCH_BYTES per device.
+ * The first call on a device does set-up: make it before any stream capture.
+ * All calls on a device share the array, so calls that overlap in time
+ * (different streams without ordering) race and give wrong results; calls in
+ * one stream are safe. */
+#define KBLAS_POSV_NOALLOC_MAX_N 256
+#define KBLAS_POSV_NOALLOC_SCRATCH_BYTES (64u << 20)
+int kblasDposv_batch_mixed_strided_noalloc(cudaStream_t stream, char side, char uplo,
+                                           const int m, const int n,
+                                           double *A, int lda, long strideA,
+                                           double *B, int ldb, long strideB,
+                                           int batchCount, int *info_array, int *iter_array);
 
 /* Status word of the last persistent launch on this handle (read by the host
  * after the stream completes): KBLAS_Success, or KBLAS_Error_Timeout if a

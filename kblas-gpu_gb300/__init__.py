@@ -85,6 +85,7 @@ _SIG = {
     "kblas_posv_batch_mixed_wsquery": (None, [P, CH, I, I, I]),
     "kblas_posv_vbatch_wsquery": (None, [P, I, I]),
     "kblasDposv_batch_mixed_strided": (I, [P, CH, CH, I, I, P, I, L, P, I, L, I, P, P]),
+    "kblasDposv_batch_mixed_strided_noalloc": (I, [P, CH, CH, I, I, P, I, L, P, I, L, I, P, P]),
     "kblasDposv_batch_mixed": (I, [P, CH, CH, I, I, P, I, P, I, I, P, P]),
     "kblasDposv_vbatch": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P]),
     "kblasDposv_vbatch_mixed": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P, P]),

@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", INC, "-I", CSRC] + ARCH
 
 LIB_UNITS = ["runtime.cu", "potrf_posv.cu", "trsm_trmm.cu", "syrk.cu", "posv_mixed.cu",
-             "posv_vbatch.cu", "cxx_overloads.cu"]
+             "posv_vbatch.cu", "posv_noalloc.cu", "cxx_overloads.cu"]
 PROBE_UNITS = ["probe.cu"]
 
 

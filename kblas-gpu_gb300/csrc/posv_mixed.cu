@@ -63,6 +63,71 @@ static int mixed_uniform(KBlasHandle *h, char side, char uplo, int m, int n, Sys
   return KBLAS_Success;
 }
 
+// The launch behind the allocation-free entry point (posv_noalloc.cu): the
+// checks and the kernel of mixed_uniform, on the caller's stream, with
+// scratch the caller owns. scratch[0, 256) is the work counter, cleared here
+// before the launch; the per-CTA slots follow it, and the grid is cut to the
+// number of slots that fit in scratch_bytes. No memory is allocated.
+int mixed_uniform_fixed_scratch(cudaStream_t stream, int device, int sm_count, int smem_optin,
+                                char side, char uplo, int m, int n, double *A, int lda,
+                                long long sA, double *B, int ldb, long long sB, int batch,
+                                int *info, int *iter, char *scratch, size_t scratch_bytes) {
+  if (is_left(side) || is_upper(uplo)) {
+    printf("(Left | Upper) POSV_BATCH is not implemented yet\n");
+    return KBLAS_NotImplemented;
+  }
+  if (!is_right(side) || !is_lower(uplo)) return KBLAS_Error_WrongInput;
+  if (m < 0 || n < 0 || batch < 0 || lda < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1))
+    return KBLAS_Error_WrongInput;
+  if (batch > 1 && (sA < (long long)lda * n || (m > 0 && sB < (long long)ldb * n)))
+    return KBLAS_Error_WrongInput;
+  if (n > 0 && batch > 0 && (!A || (m > 0 && !B))) return KBLAS_Error_WrongInput;
+  if (batch == 0) return KBLAS_Success;
+  KBlasHandle hh;  // stand-in carrying the stream and device properties only
+  hh.device_id = device;
+  hh.stream = stream;
+  hh.sm_count = sm_count;
+  hh.max_smem_optin = smem_optin;
+  if (n == 0) {
+    int st = zero_info(&hh, info, batch);
+    if (st == KBLAS_Success) st = zero_info(&hh, iter, batch);
+    return st;
+  }
+  if (n > PC_MAX_N) return KBLAS_NotSupported;
+  PosvPlan pl;
+  int st = plan_posv<true>(&hh, n, pl);
+  if (st != KBLAS_Success) return st;
+  const size_t head = 256;
+  if (!scratch || scratch_bytes < head) return KBLAS_InsufficientWorkspace;
+  if (pl.slot_bytes > 0) {
+    const size_t fit = (scratch_bytes - head) / pl.slot_bytes;
+    if (fit < 1) return KBLAS_InsufficientWorkspace;
+    if ((size_t)pl.grid > fit) pl.grid = (int)fit;
+  }
+  int *header = reinterpret_cast<int *>(scratch);
+  cudaError_t e = cudaMemsetAsync(header, 0, head, stream);
+  if (e != cudaSuccess) return cuda_check(e, "cudaMemsetAsync", __FILE__, __LINE__);
+  SysArgs sys{};
+  sys.mode = 0;
+  sys.n = n;
+  sys.m = m;
+  sys.lda = lda;
+  sys.ldb = ldb;
+  sys.A = A;
+  sys.sA = sA;
+  sys.B = B;
+  sys.sB = sB;
+  ItemArgs it{};
+  it.uniform = 1;
+  it.batch = batch;
+  it.n_uniform = n;
+  it.queue = header;
+  OutArgs out{info, iter, pl.slot_bytes ? scratch + head : nullptr, (long long)pl.slot_bytes};
+  posv_persistent_kernel<true><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
+  KGB_LAUNCH_CHECK("posv_persistent_kernel<mixed>");
+  return KBLAS_Success;
+}
+
 }  // namespace kgb
 
 using namespace kgb;
