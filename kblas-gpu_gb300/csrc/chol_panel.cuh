@@ -626,77 +626,89 @@ __device__ void team_store_panels(const Team &t, const PanelLayout &L, const T *
   }
 }
 
-// FP64 residual of up to MR right-hand sides of X*A = B: r_q = b_q - A x_q, A
-// symmetric from its lower triangle (global memory). One row per thread,
-// loads unrolled by 4 so several are in flight.
-// FP64 residual r = b - A x for one right-hand side, A symmetric from its
-// lower triangle (global memory, column-major), cut into 32 x 32 tiles. Warp
-// w takes the block columns Jb = w, w + nw, ...; walking down block column
-// Jb, lane i loads row i of tile (I, Jb) (32 independent coalesced loads),
-// adds a_ij x_j to the row sum of row I+i (kept per warp in shared memory),
-// and accumulates the mirrored products a_ij x_i per column j in registers;
-// one transpose-sum per block column turns those into the column sums. Every
-// element costs exactly its two FMAs of the symmetric product; the adds of
-// the transpose-sum are spread over a whole block column.
-// rowsum: nw x n doubles of team-shared scratch.
-static __device__ void team_residual_tiled(const Team &t, int n, const double *__restrict__ A,
+// |a| of an FP64 value as an FP32 number, from the high word only (integer
+// pipe: the FP64 -> FP32 conversion shares the scarce FP64 pipe). The
+// mantissa is truncated to 20 bits (a slight underestimate, relative error
+// below 2^-20); values below the FP32 normal range give 0, above it +inf; a
+// NaN gives NaN.
+__device__ __forceinline__ float abs_f64_as_f32(double a)
+{
+  const unsigned hi = (unsigned)__double2hiint(a) & 0x7FFFFFFFu;
+  const int e = (int)(hi >> 20);
+  if (e >= 1023 + 128) return (e == 0x7FF && ((hi & 0xFFFFFu) | (unsigned)__double2loint(a))) ? __int_as_float(0x7FC00000) : __int_as_float(0x7F800000);
+  if (e <= 1023 - 127) return 0.f;
+  return __int_as_float((int)((unsigned)(e - 1023 + 127) << 23 | (hi & 0xFFFFFu) << 3));
+}
+
+// FP64 residual r = b - A x for one right-hand side; A symmetric, its lower
+// triangle in global memory (column-major, lda). The rows are cut into blocks
+// of 32; output block I needs the tiles (I, J), J <= I, read along their rows
+// (lane = row I*32+lane, coalesced loads) and the tiles (K, I), K > I, read
+// along their columns (lane = column I*32+lane: the mirrored upper part of row
+// block I). A lane therefore accumulates its own row of the symmetric product
+// in registers: no cross-lane reduction, no masked half of the diagonal tile
+// (lane i takes a_ij from row i for j <= i and from column i for j > i), so
+// the FP64 instruction count is exactly n^2 / 32 warp FMAs for n a multiple of
+// 32. The nb^2 tile passes (nb = ceil(n / 32)) are split into equal contiguous
+// ranges over the warps; each warp writes its partial rows to rowsum (nw x n
+// doubles, team-shared), summed at the end.
+// rowabs (may be NULL): rowabs[i] += sum_j |a_ij| (FP32, truncated from the
+// FP64 high word, shared-memory atomics): the rows of the symmetric |A|,
+// computed on the integer / FP32 pipes while the FP64 pipe does the products.
+static __device__ void team_residual_owner(const Team &t, int n, const double *__restrict__ A,
                                            int lda, const double *__restrict__ b, int incb,
                                            const double *x, double *r, double *rowsum,
-                                           bool active)
+                                           float *rowabs)
 {
-  if (!active) return;
   const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
-  const int nb = (n + 31) / 32;
-  const int ntile = nb * (nb + 1) / 2;
-  // tiles in column-major order (block column Jb, then rows I >= Jb); warp w
-  // takes a contiguous, equal share, so it touches one or two block columns
-  const int t0 = (int)((long long)ntile * w / nw), t1 = (int)((long long)ntile * (w + 1) / nw);
-  double *mine = rowsum + (size_t)w * n;
-  for (int i = lane; i < n; i += 32) mine[i] = 0.0;
-  __syncwarp();
-  int Jb = 0, first = 0;  // first tile index of block column Jb
-  while (first + (nb - Jb) <= t0) {
-    first += nb - Jb;
-    Jb++;
-  }
-  int tt = t0;
-  while (tt < t1) {
-    const int J0 = Jb * 32;
-    const int Ibeg = Jb + (tt - first), Iend = min(nb, Jb + (t1 - first));
-    const double *xj = x + J0;
-    double mir[32];
-#pragma unroll
-    for (int j = 0; j < 32; j++) mir[j] = 0.0;
-    for (int I = Ibeg; I < Iend; I++) {
-      const int row = I * 32 + lane;
-      const bool rin = row < n;
-      const double xi = rin ? x[row] : 0.0;
-      double rs0 = 0.0, rs1 = 0.0;
+  const int nb = (n + 31) >> 5;
+  const int units = nb * nb;
+  const int u0 = (int)((long long)units * w / nw), u1 = (int)((long long)units * (w + 1) / nw);
+  for (int i = t.tid; i < nw * n; i += t.nt) rowsum[i] = 0.0;
+  t.sync();
+  int u = u0;
+  while (u < u1) {
+    const int I = u / nb;
+    const int uend = min(u1, (I + 1) * nb);
+    const int row = I * 32 + lane;  // output row of this lane
+    const bool rin = row < n;
+    double s0 = 0.0, s1 = 0.0;
+    float ra = 0.f;
+    for (; u < uend; u++) {
+      const int Tb = u - I * nb;  // tile column (Tb <= I) or tile row (Tb > I)
+      const int c0 = Tb * 32;
+      const double *xt = x + c0;
+      const int cw = min(32, n - c0);
 #pragma unroll
       for (int h = 0; h < 32; h += 16) {
         double a[16];
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-          const int jj = h + j;
-          const bool ok = rin && J0 + jj < n && (I > Jb || jj <= lane);
-          a[j] = ok ? A[(size_t)row + (size_t)(J0 + jj) * lda] : 0.0;
+          const int c = h + j, col = c0 + c;
+          bool ok = rin && c < cw;
+          size_t off;
+          if (Tb < I || (Tb == I && c <= lane)) off = (size_t)row + (size_t)col * lda;  // a(row, col), lower
+          else off = (size_t)col + (size_t)row * lda;                                   // a(col, row), lower
+          a[j] = ok ? A[off] : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
-          rs0 += a[j] * xj[min(h + j, n - 1 - J0)];
-          rs1 += a[j + 1] * xj[min(h + j + 1, n - 1 - J0)];
+          // x past n is not this vector's: mask it (0 * NaN would poison the sum)
+          const double x0 = (h + j < cw) ? xt[h + j] : 0.0;
+          const double x1 = (h + j + 1 < cw) ? xt[h + j + 1] : 0.0;
+          s0 += a[j] * x0;
+          s1 += a[j + 1] * x1;
         }
+        if (rowabs) {
 #pragma unroll
-        for (int j = 0; j < 16; j++)
-          if (I > Jb || h + j < lane) mir[h + j] += a[j] * xi;  // strictly lower entries only
+          for (int j = 0; j < 16; j++) ra += abs_f64_as_f32(a[j]);
+        }
       }
-      if (rin) mine[row] += rs0 + rs1;
     }
-    const double cs = warp_transpose_sum32<double>(mir);
-    if (J0 + lane < n) mine[J0 + lane] += cs;
-    tt += Iend - Ibeg;
-    first += nb - Jb;
-    Jb++;
+    if (rin) {
+      rowsum[(size_t)w * n + row] = s0 + s1;
+      if (rowabs) atomicAdd(&rowabs[row], ra);
+    }
   }
   t.sync();
   for (int i = t.tid; i < n; i += t.nt) {
@@ -705,6 +717,77 @@ static __device__ void team_residual_tiled(const Team &t, int n, const double *_
     r[i] = b[(size_t)i * incb] - s;
   }
   t.sync();
+}
+
+// y := L^{-T} L^{-1} y on panel storage by ONE warp, for a factor whose
+// diagonal squares hold the inverse of each diagonal block (lower part) and
+// its transpose (strict upper part) -- the INV form of the panel
+// factorizations. No team barrier is involved: the lanes take 32 rows at a
+// time, the diagonal blocks become 32 x 32 matrix-vector products with the
+// operand broadcast by shuffles, the updates below a block are dot products
+// along panel rows (forward) and column sums folded by a warp transpose-sum
+// (backward). Several right-hand sides run on several warps of a team at once.
+template <typename T>
+__device__ void warp_llt_solve_inv(const PanelLayout &L, const T *Ps, T *y)
+{
+  const int lane = threadIdx.x & 31;
+  const int n = L.n;
+  __syncwarp();
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    const T v = (lane < jb) ? y[J + lane] : T(0);
+    T o0 = T(0), o1 = T(0);
+#pragma unroll
+    for (int k = 0; k < 32; k += 2) {
+      const T v0 = __shfl_sync(0xffffffffu, v, k), v1 = __shfl_sync(0xffffffffu, v, k + 1);
+      if (k <= lane && lane < jb) o0 += Pp[lane + k * ld] * v0;
+      if (k + 1 <= lane && lane < jb) o1 += Pp[lane + (k + 1) * ld] * v1;
+    }
+    const T yJ = o0 + o1;
+    if (lane < jb) y[J + lane] = yJ;
+    T yc[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++) yc[c] = __shfl_sync(0xffffffffu, yJ, c);
+    for (int i = J + jb + lane; i < n; i += 32) {
+      const T *prow = Pp + (i - J);
+      T s0 = T(0), s1 = T(0);
+#pragma unroll
+      for (int c = 0; c < 32; c += 2) {
+        if (c < jb) s0 += prow[(size_t)c * ld] * yc[c];
+        if (c + 1 < jb) s1 += prow[(size_t)(c + 1) * ld] * yc[c + 1];
+      }
+      y[i] -= s0 + s1;
+    }
+    __syncwarp();
+  }
+  for (int p = L.np - 1; p >= 0; p--) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    T acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++) acc[c] = T(0);
+    for (int i0 = J + jb; i0 < n; i0 += 32) {
+      const int i = i0 + lane;
+      const T yi = (i < n) ? y[i] : T(0);
+      const T *prow = Pp + min(i - J, ld - 1);
+#pragma unroll
+      for (int c = 0; c < 32; c++)
+        if (c < jb) acc[c] += prow[(size_t)c * ld] * yi;
+    }
+    const T part = warp_transpose_sum32<T>(acc);
+    const T v = (lane < jb) ? y[J + lane] - part : T(0);
+    T o0 = T(0), o1 = T(0);
+#pragma unroll
+    for (int k = 0; k < 32; k += 2) {
+      const T v0 = __shfl_sync(0xffffffffu, v, k), v1 = __shfl_sync(0xffffffffu, v, k + 1);
+      if (k >= lane && k < jb) o0 += Pp[lane + k * ld] * v0;
+      if (k + 1 >= lane && k + 1 < jb) o1 += Pp[lane + (k + 1) * ld] * v1;
+    }
+    __syncwarp();
+    if (lane < jb) y[J + lane] = o0 + o1;
+    __syncwarp();
+  }
 }
 
 }  // namespace kgb

@@ -86,6 +86,7 @@ struct ItemArgs {
   const int4 *items;    // (n, start, count, -) into perm
   const int *perm;
   const int *nitems_p;  // number of items (device), binned batches
+  const int *split_p;   // binned: items [0, *split_p) have n > 32, the rest n <= 32
   int *queue;           // work counter (zeroed before the launch)
 };
 
@@ -311,14 +312,62 @@ static __device__ int panel_fp64_posv(const Team &t, int n, int m, int r_from, d
   return info;
 }
 
+// FP32 solves of nr right-hand sides (ys, stride n) with an INV factor: with
+// at least as many right-hand sides as warps, one warp per right-hand side
+// (no team barriers); otherwise the whole team on each in turn (a single
+// warp is latency-bound on one solve).
+static __device__ void team_solve_rhs(const Team &t, const PanelLayout &L, const float *Ps,
+                                      const float *rinv, float *ys, int nr, float *red)
+{
+  const int nw = t.nwarps();
+  if (nw > 1 && nr >= nw) {
+    for (int q = t.warp(); q < nr; q += nw) warp_llt_solve_inv<float>(L, Ps, ys + (size_t)q * L.n);
+    t.sync();
+  } else {
+    for (int q = 0; q < nr; q++) team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + (size_t)q * L.n, red, true);
+  }
+}
+
+// Plain FP64 POSV of one team's system on the panel path; FAC_SMEM as for
+// panel_mixed_posv (the FP64 factor in shared memory, else in the team's
+// global scratch).
+template <bool FAC_SMEM>
+static __device__ void panel_plain_posv(const Team &t, int n, int m, double *A, int lda,
+                                        double *B, int ldb, unsigned char *base,
+                                        double *Ps_scratch, int *info_out)
+{
+  const PanelLayout L = make_layout(n);
+  double *Ps = FAC_SMEM ? reinterpret_cast<double *>(base) : Ps_scratch;
+  unsigned char *p = base + (FAC_SMEM ? L.total() * 8 : 0);
+  double *Ld = reinterpret_cast<double *>(p); p += 32 * LDD * 8;
+  double *rinv = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+  double *y = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+  double *red = reinterpret_cast<double *>(p); p += (size_t)32 * t.nwarps() * 8;
+  int *flag = reinterpret_cast<int *>(p);
+  const int inf_ = panel_fp64_posv(t, n, m, 0, A, lda, B, ldb, Ps, Ld, rinv, y, red, flag);
+  if (info_out && t.tid == 0) *info_out = inf_;
+}
+
+// Phase clock hooks of the mixed panel path for profiling builds; empty in
+// the library.
+#ifndef KGB_PHASE_BEGIN
+#define KGB_PHASE_BEGIN(t)
+#define KGB_PHASE_MARK(t, k)
+#endif
+
+// FAC_SMEM: the FP32 factor lives in the team's shared memory (else in its
+// global scratch slot). A compile-time choice, so that every access to a
+// shared-memory factor compiles to a shared-memory instruction rather than a
+// generic one.
+template <bool FAC_SMEM>
 static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, int lda, double *B,
-                                 int ldb, unsigned char *base, bool fac_smem, float *Ps_scratch,
+                                 int ldb, unsigned char *base, float *Ps_scratch,
                                  double *Ps64_scratch, int *info_out, int *iter_out)
 {
   const PanelLayout L = make_layout(n);
   const int nw = t.nwarps();
-  float *Ps = fac_smem ? reinterpret_cast<float *>(base) : Ps_scratch;
-  unsigned char *p = base + (fac_smem ? L.total() * 4 : 0);
+  float *Ps = FAC_SMEM ? reinterpret_cast<float *>(base) : Ps_scratch;
+  unsigned char *p = base + (FAC_SMEM ? L.total() * 4 : 0);
   double *Ld64 = reinterpret_cast<double *>(p); p += 32 * LDD * 8;
   float *Ld = reinterpret_cast<float *>(Ld64);
   double *rinv64 = reinterpret_cast<double *>(p); p += (size_t)n * 8;
@@ -326,12 +375,13 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   float *scl = reinterpret_cast<float *>(p); p += (size_t)n * 4;
   int *sh = reinterpret_cast<int *>(p); p += (size_t)n * 4;
   float *ys = reinterpret_cast<float *>(p); p += (size_t)PC_MR * n * 4;
-  p = reinterpret_cast<unsigned char *>(((uintptr_t)p + 7) & ~(uintptr_t)7);
+  p = base + (((size_t)(p - base) + 7) & ~(size_t)7);  // offset arithmetic keeps p shared
   double *x = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
   double *r = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
   double *colsum = reinterpret_cast<double *>(p); p += (size_t)nw * n * 8;
   double *red = reinterpret_cast<double *>(p); p += (size_t)32 * nw * 8;
   int *flag = reinterpret_cast<int *>(p);
+  KGB_PHASE_BEGIN(t);
 
   // 1. scales
   int bad = 0;
@@ -341,20 +391,19 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
     sh[i] = e;
   }
   t.sync();
-  // 2. stage As = S A S (FP32) with the row sums of |A| (ys as scratch), factor
-  float *rowabs = ys;
-  for (int i = t.tid; i < n; i += t.nt) rowabs[i] = 0.f;
+  // 2. stage As = S A S (FP32), factor
+  team_load_panels<float, true>(t, L, A, lda, Ps, sh, nullptr);
   t.sync();
-  team_load_panels<float, true>(t, L, A, lda, Ps, sh, rowabs);
-  t.sync();
-  float an_local = 0.f;
-  for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
-  const float an = team_max<float>(t, an_local, reinterpret_cast<float *>(red));
-  const double anorm = (double)an * (1.0 + 1e-6 * n);
+  KGB_PHASE_MARK(t, 0);
+  // ||A||_inf comes from the first residual (row sums of |A| on the spare
+  // integer / FP32 issue slots of that FP64-bound pass); an underestimate
+  // only makes the backward-error test stricter
+  double anorm = -1.0;
   const float ftol = (float)n * 5.9604645e-08f;  // n * 2^-24
   const int fail = (t.nt >= 64)
                        ? team_potrf_panel_la<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag)
                        : team_potrf_panel<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag, true);
+  KGB_PHASE_MARK(t, 1);
   const int any_bad = team_any(t, bad, reinterpret_cast<int *>(red));
   bool need_fb = fail != 0 || any_bad;
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
@@ -362,14 +411,16 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   // 3. solve + refine, PC_MR right-hand sides at a time
   for (int r0 = 0; r0 < m && !need_fb; r0 += PC_MR) {
     const int nr = min(PC_MR, m - r0);
-    for (int q = 0; q < nr; q++) {
+    // one warp per right-hand side for the FP32 solves
+    for (int q = 0; q < nr; q++)
       for (int i = t.tid; i < n; i += t.nt)
         ys[q * n + i] = f64_to_f32_scaled(B[(size_t)(r0 + q) + (size_t)i * ldb], sh[i]);
-      t.sync();
-      team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
+    t.sync();
+    team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red));
+    for (int q = 0; q < nr; q++)
       for (int i = t.tid; i < n; i += t.nt) x[q * n + i] = (double)(ys[q * n + i] * scl[i]);
-      t.sync();
-    }
+    t.sync();
+    KGB_PHASE_MARK(t, 2);
     double bmax[PC_MR];
     for (int q = 0; q < PC_MR; q++) {
       double bm = 0.0;
@@ -381,8 +432,18 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
     bool converged = false;
     int step = 0;
     for (;;) {
-      for (int q = 0; q < nr; q++)
-        team_residual_tiled(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n, colsum, true);
+      for (int q = 0; q < nr; q++) {
+        float *rowabs = (anorm < 0.0 && q == 0) ? ys : nullptr;  // ys is free here
+        if (rowabs)
+          for (int i = t.tid; i < n; i += t.nt) rowabs[i] = 0.f;
+        team_residual_owner(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n, colsum, rowabs);
+        if (rowabs) {
+          float an_local = 0.f;
+          for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
+          anorm = (double)team_max<float>(t, an_local, reinterpret_cast<float *>(red));
+        }
+      }
+      KGB_PHASE_MARK(t, 3);
       double eta = 0.0;
       for (int q = 0; q < nr; q++) {
         double rm = 0.0, xm = 0.0;
@@ -404,13 +465,14 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
       }
       if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) break;
       eta_prev = eta;
-      for (int q = 0; q < nr; q++) {
+      for (int q = 0; q < nr; q++)
         for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = f64_to_f32_scaled(r[q * n + i], sh[i]);
-        t.sync();
-        team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + q * n, reinterpret_cast<float *>(red), true);
+      t.sync();
+      team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red));
+      for (int q = 0; q < nr; q++)
         for (int i = t.tid; i < n; i += t.nt) x[q * n + i] += (double)(ys[q * n + i] * scl[i]);
-        t.sync();
-      }
+      t.sync();
+      KGB_PHASE_MARK(t, 4);
       step++;
     }
     steps_used = max(steps_used, step);
@@ -429,6 +491,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   if (need_fb)
     info = panel_fp64_posv(t, n, m, fb_from, A, lda, B, ldb, Ps64_scratch, Ld64, rinv64, x, red,
                            flag);
+  KGB_PHASE_MARK(t, 5);
   if (t.tid == 0) {
     if (info_out) *info_out = need_fb ? info : 0;
     if (iter_out) *iter_out = need_fb ? fb_code : steps_used;
@@ -473,29 +536,37 @@ __device__ __forceinline__ void prefetch_item(const SysArgs &sys, const ItemArgs
     for (const char *a = lo; a < hi; a += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
   }
 }
-template <bool MIXED>
+// PATHS selects the code compiled in: bit 0 the register path (n <= 32), bit
+// 1 the panel path (n > 32). A kernel holding one path only gets that path's
+// register allocation (each path alone fits the register file; together they
+// spill), so the binned launcher runs the two paths as two launches over the
+// two item ranges: [0, *split_p) panel items, [*split_p, *nitems_p) register
+// items.
+template <bool MIXED, int PATHS = 3>
 __global__ void __launch_bounds__(PC_NT, 1)
 posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int smem_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_item;
-  long long nitems;
+  long long first = 0, nitems;
   if (it.uniform) {
     const int spi = cfg.spi[pc_class(cfg, it.n_uniform)];
     nitems = (it.batch + spi - 1) / spi;
   } else {
     nitems = *it.nitems_p;
+    if (PATHS == 2) nitems = *it.split_p;
+    if (PATHS == 1) first = *it.split_p;
   }
   char *slot = out.scratch ? out.scratch + (size_t)blockIdx.x * out.slot_bytes : nullptr;
 
-  if (threadIdx.x == 0) s_item = atomicAdd(it.queue, 1);
+  if (threadIdx.x == 0) s_item = (int)first + atomicAdd(it.queue, 1);
   for (;;) {
     __syncthreads();
     const long long q = s_item;
     __syncthreads();
     if (q >= nitems) break;
     // claim the next item now and warm L2 with its matrices
-    if (threadIdx.x == 0) s_item = atomicAdd(it.queue, 1);
+    if (threadIdx.x == 0) s_item = (int)first + atomicAdd(it.queue, 1);
     __syncthreads();
     if (s_item < nitems) prefetch_item(sys, it, cfg, s_item);
     int n, start, count;
@@ -518,6 +589,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
     int *info_p = (active && out.info) ? out.info + sidx : nullptr;
     int *iter_p = (active && out.iter) ? out.iter + sidx : nullptr;
     if (n <= 32) {
+      if constexpr ((PATHS & 1) != 0) {
       // register path: every segment of each warp runs, idle ones on no data
 #define KGB_SMALL(WW)                                                                      \
   if (MIXED) {                                                                             \
@@ -536,7 +608,9 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
         KGB_SMALL(32)
       }
 #undef KGB_SMALL
+      }
     } else if (active) {
+      if constexpr ((PATHS & 2) != 0) {
       const Team t{(int)(threadIdx.x % TS), TS, 1 + team_id};
       const PanelLayout L = make_layout(n);
       // scratch slot: FP64 panels of every team, then FP32 ones
@@ -546,17 +620,16 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
                                (size_t)team_id * L.total()
                          : nullptr;
       if (MIXED) {
-        panel_mixed_posv(t, n, m, A, lda, B, ldb, base, fac_smem, P32s, P64s, info_p, iter_p);
+        if (fac_smem)
+          panel_mixed_posv<true>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p);
+        else
+          panel_mixed_posv<false>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p);
       } else {
-        double *Ps = fac_smem ? reinterpret_cast<double *>(base) : P64s;
-        unsigned char *p = base + (fac_smem ? L.total() * 8 : 0);
-        double *Ld = reinterpret_cast<double *>(p); p += 32 * LDD * 8;
-        double *rinv = reinterpret_cast<double *>(p); p += (size_t)n * 8;
-        double *y = reinterpret_cast<double *>(p); p += (size_t)n * 8;
-        double *red = reinterpret_cast<double *>(p); p += (size_t)32 * (TS / 32) * 8;
-        int *flag = reinterpret_cast<int *>(p);
-        const int inf_ = panel_fp64_posv(t, n, m, 0, A, lda, B, ldb, Ps, Ld, rinv, y, red, flag);
-        if (info_p && t.tid == 0) *info_p = inf_;
+        if (fac_smem)
+          panel_plain_posv<true>(t, n, m, A, lda, B, ldb, base, P64s, info_p);
+        else
+          panel_plain_posv<false>(t, n, m, A, lda, B, ldb, base, P64s, info_p);
+      }
       }
     }
     __syncthreads();

@@ -65,7 +65,10 @@ static inline bool cfg_valid(const PosvCfg &c) {
   return c.nmax[PC_NCLS - 1] >= PC_MAX_N;
 }
 
-template <bool MIXED>
+// Launch plan of posv_persistent_kernel<MIXED, PATHS> for orders up to max_n:
+// shared memory = the largest need over the size classes that kernel serves
+// (register path: orders <= 32; panel path: orders > 32).
+template <bool MIXED, int PATHS = 3>
 static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
   pl.cfg = current_cfg(MIXED);
   if (!cfg_valid(pl.cfg)) return KBLAS_WrongConfig;
@@ -76,13 +79,22 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
     const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
     if (nhi < nlo) continue;
     const int nteams = PC_NT / pl.cfg.ts[c];
-    size_t b = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], true);
-    if (b > budget) b = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], false);
+    size_t b = 0;
+    if ((PATHS & 1) && nlo <= 32) {
+      const size_t b1 = (size_t)nteams * team_smem_bytes<MIXED>(nhi < 32 ? nhi : 32, pl.cfg.ts[c], true);
+      if (b1 > b) b = b1;
+    }
+    if ((PATHS & 2) && nhi > 32) {
+      size_t b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], true);
+      if (b2 > budget) b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], false);
+      if (b2 > b) b = b2;
+    }
     if (b > budget) return KBLAS_NotSupported;
     if (b > smem) smem = b;
   }
+  if (smem == 0) smem = 16;
   pl.smem = (int)smem;
-  auto kern = posv_persistent_kernel<MIXED>;
+  auto kern = posv_persistent_kernel<MIXED, PATHS>;
   int st = set_smem(kern, smem);
   if (st != KBLAS_Success) return st;
   int per_sm = 0;
@@ -90,14 +102,15 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
       per_sm < 1)
     per_sm = 1;
   pl.grid = h->sm_count * per_sm;
-  pl.slot_bytes = posv_slot_bytes(pl.cfg, max_n);
+  pl.slot_bytes = (PATHS & 2) ? posv_slot_bytes(pl.cfg, max_n) : 0;
   return KBLAS_Success;
 }
 
 // Device workspace layout shared by the uniform mixed and the variable-size
 // routines (offsets in bytes from the start of the handle's device data).
 struct PosvWs {
-  size_t header = 0;   // int[64]: [0] queue, [1] item count
+  size_t header = 0;   // int[64]: [0] panel-path queue, [1] item count, [2] register-path
+                       // queue, [3] panel items (items with n > 32 come first)
   size_t cnt = 0;      // int[max_n + 1]   systems per order n
   size_t off = 0;      // int[max_n + 1]   first slot of order n in perm
   size_t ioff = 0;     // int[max_n + 1]   first item of order n

@@ -20,7 +20,8 @@ TuneOverride &tune_override() {
 size_t mixed_posv_ws_bytes(KBlasHandle *h, int n, long long batch) {
   if (batch <= 0 || n <= 0) return 0;
   PosvPlan pl;
-  if (plan_posv<true>(h, n, pl) != KBLAS_Success) return 0;
+  const int st = n > 32 ? plan_posv<true, 2>(h, n, pl) : plan_posv<true, 1>(h, n, pl);
+  if (st != KBLAS_Success) return 0;
   return posv_ws_layout(n, batch, false, pl).total;
 }
 
@@ -42,7 +43,7 @@ static int mixed_uniform(KBlasHandle *h, char side, char uplo, int m, int n, Sys
   }
   if (n > PC_MAX_N) return KBLAS_NotSupported;
   PosvPlan pl;
-  int st = plan_posv<true>(h, n, pl);
+  int st = n > 32 ? plan_posv<true, 2>(h, n, pl) : plan_posv<true, 1>(h, n, pl);
   if (st != KBLAS_Success) return st;
   const PosvWs ws = posv_ws_layout(n, batch, false, pl);
   if (ws.total > h->ws.allocated.d_data_bytes || !h->ws.d_data) return KBLAS_InsufficientWorkspace;
@@ -58,7 +59,10 @@ static int mixed_uniform(KBlasHandle *h, char side, char uplo, int m, int n, Sys
   OutArgs out{info, iter, base + ws.scratch, (long long)pl.slot_bytes};
   sys.n = n;
   sys.m = m;
-  posv_persistent_kernel<true><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+  if (n > 32)
+    posv_persistent_kernel<true, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+  else
+    posv_persistent_kernel<true, 1><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
   KGB_LAUNCH_CHECK("posv_persistent_kernel<mixed>");
   return KBLAS_Success;
 }
@@ -95,7 +99,7 @@ int mixed_uniform_fixed_scratch(cudaStream_t stream, int device, int sm_count, i
   }
   if (n > PC_MAX_N) return KBLAS_NotSupported;
   PosvPlan pl;
-  int st = plan_posv<true>(&hh, n, pl);
+  int st = n > 32 ? plan_posv<true, 2>(&hh, n, pl) : plan_posv<true, 1>(&hh, n, pl);
   if (st != KBLAS_Success) return st;
   const size_t head = 256;
   if (!scratch || scratch_bytes < head) return KBLAS_InsufficientWorkspace;
@@ -123,7 +127,10 @@ int mixed_uniform_fixed_scratch(cudaStream_t stream, int device, int sm_count, i
   it.n_uniform = n;
   it.queue = header;
   OutArgs out{info, iter, pl.slot_bytes ? scratch + head : nullptr, (long long)pl.slot_bytes};
-  posv_persistent_kernel<true><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
+  if (n > 32)
+    posv_persistent_kernel<true, 2><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
+  else
+    posv_persistent_kernel<true, 1><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
   KGB_LAUNCH_CHECK("posv_persistent_kernel<mixed>");
   return KBLAS_Success;
 }

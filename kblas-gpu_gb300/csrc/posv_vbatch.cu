@@ -53,8 +53,9 @@ __global__ void vb_plan(int max_n, const int *cnt, int *off, int *ioff, int4 *it
 {
   // prefix sums over n, largest n first (max_n <= 1024: one thread suffices)
   if (threadIdx.x == 0) {
-    int o = 0, io = 0;
+    int o = 0, io = 0, split = -1;
     for (int nn = max_n; nn >= 1; nn--) {
+      if (split < 0 && nn <= 32) split = io;  // items of orders > 32 come first
       off[nn] = o;
       ioff[nn] = io;
       const int c = cnt[nn];
@@ -63,6 +64,7 @@ __global__ void vb_plan(int max_n, const int *cnt, int *off, int *ioff, int4 *it
       io += (c + spi - 1) / spi;
     }
     header[1] = io;
+    header[3] = split < 0 ? io : split;
   }
   __syncthreads();
   for (int nn = 1 + threadIdx.x; nn <= max_n; nn += blockDim.x) {
@@ -90,12 +92,24 @@ __global__ void vb_scatter(long long batch, const int *n, const int *m, const in
   }
 }
 
+// Plans of the two launches: the panel path (orders > 32; carries the
+// per-CTA scratch) and the register path (orders <= 32).
+template <bool MIXED>
+static int plan_vbatch(KBlasHandle *h, int max_n, PosvPlan &panel, PosvPlan &reg) {
+  int st = plan_posv<MIXED, 1>(h, max_n < 32 ? max_n : 32, reg);
+  if (st != KBLAS_Success) return st;
+  if (max_n > 32) return plan_posv<MIXED, 2>(h, max_n, panel);
+  panel = reg;
+  panel.slot_bytes = 0;
+  return KBLAS_Success;
+}
+
 size_t vbatch_ws_bytes(KBlasHandle *h, int max_n, long long batch, bool mixed) {
   if (batch <= 0 || max_n <= 0 || max_n > PC_MAX_N) return 0;
-  PosvPlan pl;
-  int st = mixed ? plan_posv<true>(h, max_n, pl) : plan_posv<false>(h, max_n, pl);
+  PosvPlan panel, reg;
+  int st = mixed ? plan_vbatch<true>(h, max_n, panel, reg) : plan_vbatch<false>(h, max_n, panel, reg);
   if (st != KBLAS_Success) return 0;
-  return posv_ws_layout(max_n, batch, true, pl).total;
+  return posv_ws_layout(max_n, batch, true, panel).total;
 }
 
 template <bool MIXED>
@@ -115,8 +129,8 @@ static int vbatch(KBlasHandle *h, char side, char uplo, int *m, int *n, int max_
     int st = zero_info(h, info, batch);
     return st == KBLAS_Success ? zero_info(h, iter, batch) : st;
   }
-  PosvPlan pl;
-  int st = plan_posv<MIXED>(h, max_n, pl);
+  PosvPlan pl, preg;
+  int st = plan_vbatch<MIXED>(h, max_n, pl, preg);
   if (st != KBLAS_Success) return st;
   const PosvWs ws = posv_ws_layout(max_n, batch, true, pl);
   if (ws.total > h->ws.allocated.d_data_bytes || !h->ws.d_data) return KBLAS_InsufficientWorkspace;
@@ -155,9 +169,16 @@ static int vbatch(KBlasHandle *h, char side, char uplo, int *m, int *n, int max_
   it.items = items;
   it.perm = perm;
   it.nitems_p = header + 1;
-  it.queue = header;
+  it.split_p = header + 3;
   OutArgs out{info, MIXED ? iter : nullptr, base + ws.scratch, (long long)pl.slot_bytes};
-  posv_persistent_kernel<MIXED><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+  // orders > 32 first (largest first), then orders <= 32 on the register path
+  if (max_n > 32) {
+    it.queue = header;
+    posv_persistent_kernel<MIXED, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+    KGB_LAUNCH_CHECK("posv_persistent_kernel");
+  }
+  it.queue = header + 2;
+  posv_persistent_kernel<MIXED, 1><<<preg.grid, PC_NT, preg.smem, h->stream>>>(sys, it, out, preg.cfg, preg.smem);
   KGB_LAUNCH_CHECK("posv_persistent_kernel");
   return KBLAS_Success;
 }
