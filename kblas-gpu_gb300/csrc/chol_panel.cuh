@@ -23,6 +23,12 @@
 
 namespace kgb {
 
+// Sub-phase clock hooks for profiling builds; empty in the library.
+#ifndef KGB_SUBPHASE_BEGIN
+#define KGB_SUBPHASE_BEGIN(t)
+#define KGB_SUBPHASE_MARK(t, k)
+#endif
+
 constexpr int PNB = 32;  // panel width
 constexpr int LDD = 33;  // row stride of the diagonal-block copy (conflict free)
 
@@ -85,38 +91,52 @@ __device__ __forceinline__ int warp_chol_rot(T (&v)[32], int jb, T tol, T *Lrow,
 }
 
 // Warp-level inverse of a factored diagonal block held in the panel's
-// diagonal square (lower part, column-major, leading dimension ld): lane j
-// computes column j of X = L^{-1} by forward substitution (X[k] = 0 above the
-// diagonal), reading L with broadcast loads; then X replaces L in the lower
-// part and X^T fills the strict upper part.
+// diagonal square (lower part, column-major, leading dimension ld a multiple
+// of 4, 16-byte aligned columns): lane j computes column j of X = L^{-1} by a
+// right-looking sweep in registers (x_i = b_i / L(i,i); b_r -= L(r,i) x_i for
+// r > i), reading column i of L as broadcast 128-bit loads; then X replaces L
+// in the lower part and X^T fills the strict upper part. The sweep is fully
+// unrolled: it runs on every warp of a team at once (one block each), so the
+// warps share the instruction fetch of the long straight-line code.
 template <typename T>
 __device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T *rinvJ)
 {
   const int lane = threadIdx.x & 31;
-  T X[32];
+  T b[32];
 #pragma unroll
-  for (int k = 0; k < 32; k++) X[k] = T(0);
-  for (int i = 0; i < jb; i++) {
-    T s0 = (i == lane) ? T(1) : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+  for (int i = 0; i < 32; i++) b[i] = (i == lane) ? T(1) : T(0);
 #pragma unroll
-    for (int k = 0; k < 32; k += 4) {
-      if (k < i) s0 -= Pp[i + k * ld] * X[k];
-      if (k + 1 < i) s1 -= Pp[i + (k + 1) * ld] * X[k + 1];
-      if (k + 2 < i) s2 -= Pp[i + (k + 2) * ld] * X[k + 2];
-      if (k + 3 < i) s3 -= Pp[i + (k + 3) * ld] * X[k + 3];
+  for (int i = 0; i < 32; i++) {
+    if (i < jb) {
+      const T xi = b[i] * rinvJ[i];
+      b[i] = xi;
+#pragma unroll
+      for (int r0 = (i + 1) & ~3; r0 < 32; r0 += 4) {
+        if (r0 < jb) {
+          T q0, q1, q2, q3;
+          if (sizeof(T) == 4) {
+            const float4 q = *reinterpret_cast<const float4 *>(Pp + r0 + i * ld);
+            q0 = q.x; q1 = q.y; q2 = q.z; q3 = q.w;
+          } else {
+            const double2 qa = *reinterpret_cast<const double2 *>(Pp + r0 + i * ld);
+            const double2 qb = *reinterpret_cast<const double2 *>(Pp + r0 + 2 + i * ld);
+            q0 = qa.x; q1 = qa.y; q2 = qb.x; q3 = qb.y;
+          }
+          if (r0 + 0 > i) b[r0 + 0] -= q0 * xi;
+          if (r0 + 1 > i) b[r0 + 1] -= q1 * xi;
+          if (r0 + 2 > i) b[r0 + 2] -= q2 * xi;
+          if (r0 + 3 > i) b[r0 + 3] -= q3 * xi;
+        }
+      }
     }
-    const T xi = ((s0 + s1) + (s2 + s3)) * rinvJ[i];
-#pragma unroll
-    for (int k = 0; k < 32; k++)
-      if (k == i) X[k] = xi;
   }
-  __syncwarp();
+  __syncwarp();  // every lane is done reading L
   if (lane < jb) {
 #pragma unroll
-    for (int k = 0; k < 32; k++) {
-      if (k < jb) {
-        if (k >= lane) Pp[k + lane * ld] = X[k];
-        if (k > lane) Pp[lane + k * ld] = X[k];
+    for (int i = 0; i < 32; i++) {
+      if (i < jb) {
+        if (i > lane) Pp[lane + i * ld] = b[i];   // X^T, strict upper part
+        if (i >= lane) Pp[i + lane * ld] = b[i];  // X, lower part
       }
     }
   }
@@ -330,8 +350,10 @@ __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T
                                    T tol, int *flag)
 {
   const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  KGB_SUBPHASE_BEGIN(t);
   if (w == 0) warp_factor_diag<T, CHECK_INF>(L, 0, Ps, Ld2, rinv, tol, flag);
   t.sync();
+  KGB_SUBPHASE_MARK(t, 8);
   int fail = *flag;
   for (int p = 0; p < L.np && !fail; p++) {
     const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
@@ -363,6 +385,7 @@ __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T
         if (c < jb) Pp[i + c * ld] = x[c];
     }
     t.sync();
+    KGB_SUBPHASE_MARK(t, 9);
     // (c) trailing update; warp 0 takes the next diagonal block first
     if (w == 0) {
       if (p + 1 < L.np) {
@@ -397,12 +420,14 @@ __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T
       }
     }
     t.sync();
+    KGB_SUBPHASE_MARK(t, 10);
     fail = *flag;
   }
   if (INV && !fail) {
     for (int p = w; p < L.np; p += nw) warp_invert_diag<T>(Ps + L.base(p), L.ldp(p), L.jb(p), rinv + p * PNB);
     t.sync();
   }
+  KGB_SUBPHASE_MARK(t, 11);
   (void)lane;
   return fail;
 }
