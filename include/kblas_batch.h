@@ -204,9 +204,11 @@ int kblasDposv_vbatch_mixed(kblasHandle_t handle, char side, char uplo,
 
 /* Override the launch-shape table of the persistent POSV kernels (mixed != 0:
  * the mixed-precision table, else the plain FP64 one): per size class, the
- * largest order n of the class, the team size in threads (2..256, a power of
- * two) and the systems per work item. Six entries each; NULL restores the
- * table compiled into the library. Used by the committed autotuner. */
+ * largest order n of the class, the team size in threads (8..256, a power of
+ * two) and the systems per work item. KBLAS_POSV_TUNING_CLASSES entries each;
+ * NULL restores the table compiled into the library. Used by the committed
+ * autotuner. */
+#define KBLAS_POSV_TUNING_CLASSES 8
 int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi);
 
 /* Allocation-free mixed-precision POSV (no counterpart in the reference).

@@ -1,7 +1,7 @@
 """Autotuner of the persistent POSV launch shapes (writes csrc/tuning_table.h).
 
 The persistent POSV kernels (plain FP64 and mixed precision) split orders into
-six size classes; per class the table gives the team size (threads per system)
+eight size classes; per class the table gives the team size (threads per system)
 and the systems per work item. A work item is spread over the teams of one
 CTA, one system per team, so the useful item size is the number of teams
 (256 / team size); the choice that matters is the team size. For each class
@@ -25,14 +25,20 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 NT = 256                                  # threads per CTA of the persistent kernels
-NMAX = [8, 16, 32, 64, 128, 1024]         # class upper bounds (last: largest supported order)
-CLASS_TOP = [8, 16, 32, 64, 128, 256]     # orders swept in each class (last capped at 256)
+# class upper bounds (last: largest supported order); 64, 96 and 176 are
+# about where the factors of 8, 4 and 2 teams per CTA stop fitting in shared
+# memory
+NMAX = [8, 16, 32, 64, 96, 128, 176, 1024]
+CLASS_TOP = [8, 16, 32, 64, 96, 128, 176, 256]  # orders swept per class (last capped at 256)
+NCLS = len(NMAX)
 CANDIDATES = [                            # team sizes accepted per class (W >= n for n <= 32)
     [8, 16, 32],
     [16, 32],
     [32],
+    [32, 64, 128],
     [32, 64, 128, 256],
     [32, 64, 128, 256],
+    [64, 128, 256],
     [64, 128, 256],
 ]
 
@@ -122,7 +128,7 @@ def time_call(torch, kb, h, cb, mixed, reps):
 
 def set_table(kb, mixed, ts, spi):
     C = __import__("ctypes")
-    arr = lambda v: (C.c_int * 6)(*v)
+    arr = lambda v: (C.c_int * NCLS)(*v)
     st = kb.lib().kblasSetPosvTuning(1 if mixed else 0, arr(NMAX), arr(ts), arr(spi))
     if st != 1:
         raise RuntimeError(f"kblasSetPosvTuning rejected ts={ts} spi={spi}")
@@ -133,17 +139,16 @@ def tune(torch, kb, reps=5, log=print):
     h = kb.Handle(stream=torch.cuda.current_stream().cuda_stream)
     out = {}
     batches = []
-    for c in range(6):
+    for c in range(NCLS):
         lo = 1 if c == 0 else CLASS_TOP[c - 1] + 1
         batches.append(ClassBatch(torch, lo, CLASS_TOP[c], seed=c))
     try:
         for form in ("mixed", "plain"):
             mixed = form == "mixed"
-            defaults = {"mixed": ([8, 16, 32, 32, 128, 256], [32, 16, 8, 8, 2, 1]),
-                        "plain": ([8, 16, 32, 32, 128, 256], [32, 16, 8, 8, 2, 1])}[form]
-            best_ts, best_spi = list(defaults[0]), list(defaults[1])
+            best_ts = [8, 16, 32, 32, 64, 128, 128, 256]
+            best_spi = [NT // t for t in best_ts]
             ms_table = {}
-            for c in range(6):
+            for c in range(NCLS):
                 cb = batches[c]
                 res = {}
                 for ts in CANDIDATES[c]:

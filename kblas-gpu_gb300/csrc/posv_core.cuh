@@ -38,7 +38,7 @@
 namespace kgb {
 
 constexpr int PC_NT = 256;     // threads per persistent CTA
-constexpr int PC_NCLS = 6;     // size classes
+constexpr int PC_NCLS = 8;     // size classes (KBLAS_POSV_TUNING_CLASSES)
 constexpr int PC_MR = 4;       // right-hand sides per residual sweep (panel path)
 constexpr int PC_ITMAX = 12;   // refinement step cap
 constexpr double PC_EPS64 = 1.1102230246251565e-16;

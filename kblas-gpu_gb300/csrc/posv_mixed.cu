@@ -12,6 +12,8 @@
 
 namespace kgb {
 
+static_assert(PC_NCLS == KBLAS_POSV_TUNING_CLASSES, "size-class count of the tuning API");
+
 TuneOverride &tune_override() {
   static TuneOverride o;
   return o;
@@ -172,8 +174,8 @@ int kblasDposv_batch_mixed(kblasHandle_t h, char side, char uplo, const int m, c
 }
 
 // Tuning-table override (used by the autotuner to time candidate shapes
-// without rebuilding). mixed selects the table; nmax/ts/spi hold 6 entries
-// each. Passing NULL arrays restores the compiled table.
+// without rebuilding). mixed selects the table; nmax/ts/spi hold
+// KBLAS_POSV_TUNING_CLASSES entries each. Passing NULL arrays restores the compiled table.
 int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi) {
   TuneOverride &o = tune_override();
   const int k = mixed ? 1 : 0;

@@ -265,9 +265,10 @@ def test_vbatch_needs_workspace(gpu, handle, kb):
 def test_tuning_override_roundtrip(gpu, handle, kb, wl, orc):
     """A different launch-shape table gives the same (correct) answers."""
     L = kb.lib()
-    arr = lambda v: (ctypes.c_int * 6)(*v)
-    assert L.kblasSetPosvTuning(1, arr([8, 16, 32, 64, 128, 1024]), arr([8, 16, 32, 64, 256, 256]),
-                                arr([32, 16, 8, 4, 1, 1])) == 1
+    arr = lambda v: (ctypes.c_int * 8)(*v)  # KBLAS_POSV_TUNING_CLASSES
+    nmax = [8, 16, 32, 64, 96, 128, 176, 1024]
+    assert L.kblasSetPosvTuning(1, arr(nmax), arr([8, 16, 32, 64, 64, 256, 256, 256]),
+                                arr([32, 16, 8, 4, 4, 1, 1, 1])) == 1
     try:
         n, m, batch = 40, 2, 30
         a = wl.spd_shifted(batch, n, seed=21)
@@ -279,7 +280,7 @@ def test_tuning_override_roundtrip(gpu, handle, kb, wl, orc):
         assert L.kblasSetPosvTuning(1, None, None, None) == 1
     # invalid tables are rejected: a register-path team narrower than its
     # orders, a team size that is not a power of two
-    assert L.kblasSetPosvTuning(1, arr([8, 16, 32, 64, 128, 1024]), arr([8, 8, 32, 64, 256, 256]),
-                                arr([32, 32, 8, 4, 1, 1])) == kb.KBLAS_Error_WrongInput
-    assert L.kblasSetPosvTuning(1, arr([8, 16, 32, 64, 128, 1024]), arr([3, 16, 32, 64, 256, 256]),
-                                arr([32, 16, 8, 4, 1, 1])) == kb.KBLAS_Error_WrongInput
+    assert L.kblasSetPosvTuning(1, arr(nmax), arr([8, 8, 32, 64, 64, 256, 256, 256]),
+                                arr([32, 32, 8, 4, 4, 1, 1, 1])) == kb.KBLAS_Error_WrongInput
+    assert L.kblasSetPosvTuning(1, arr(nmax), arr([3, 16, 32, 64, 64, 256, 256, 256]),
+                                arr([32, 16, 8, 4, 4, 1, 1, 1])) == kb.KBLAS_Error_WrongInput
