@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "batched POSV solves/s at backward err ≤10·n·eps64: mixed-prec vs plain FP64"
 EPS64 = 2.0 ** -53
+E2E_CHUNKS = 16
 WORKLOAD = ("variable-size DPOSV: 100000 SPD systems, n log-uniform integer 8..256, "
             "A = G G^T + n I, 1 RHS, pointer arrays, 1% indefinite (one eigenvalue flipped)")
 
@@ -431,6 +432,7 @@ def main():
     acc_mixed = accuracy_check(orc, w, torch)
     it = w.iter.cpu().numpy()
     info = w.info.cpu().numpy()
+    x_mixed = w.B.cpu()
     # ---- plain FP64 ----
     t_fp64 = timed_steps(torch, lambda: call_vbatch(kb, h, w, False), lambda: w.restore(full=True),
                          max(2, args.steps // 2), 2, stream)
@@ -444,14 +446,64 @@ def main():
     hX = torch.empty_like(hB, pin_memory=True)
     hinfo = torch.empty(w.batch, dtype=torch.int32, pin_memory=True)
 
+    # The batch is split into E2E_CHUNKS pieces that are contiguous in the
+    # matrix pool (equal bytes); the host->device copy of piece k+1 runs on a
+    # copy stream while piece k is solved on the handle's stream -- the usual
+    # way to feed a GPU library from host memory, through the same C ABI call.
+    order = np.argsort(w.offs, kind="stable")
+    nbytes = w.ns[order].astype(np.int64) ** 2
+    cum = np.cumsum(nbytes)
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / E2E_CHUNKS)) + 1
+                  for k in range(1, E2E_CHUNKS)] + [w.batch]
+    chunks = []
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        if hi <= lo:
+            continue
+        idx = order[lo:hi]
+        it_ = torch.from_numpy(idx).to("cuda")
+        a_lo = int(w.offs[idx[0]])
+        a_hi = int(w.offs[idx[-1]]) + int(w.ns[idx[-1]]) ** 2
+        c = {"n": len(idx), "a": (a_lo, a_hi), "max_n": int(w.ns[idx].max()),
+             "pA": w.pA[it_], "pB": w.pB[it_], "dn": w.dn[it_], "dm": w.dm[it_],
+             "dldb": w.dldb[it_], "info": torch.zeros(len(idx), dtype=torch.int32, device="cuda"),
+             "iter": torch.zeros(len(idx), dtype=torch.int32, device="cuda"),
+             "hinfo": torch.empty(len(idx), dtype=torch.int32, pin_memory=True),
+             "ev": torch.cuda.Event()}
+        kb.lib().kblas_posv_vbatch_wsquery(h.ptr, c["max_n"], c["n"])
+        chunks.append(c)
+    kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
+    copy_stream = torch.cuda.Stream()
+    ev_b = torch.cuda.Event()
+
     def e2e_step():
-        w.A.copy_(hA, non_blocking=True)
-        w.B.copy_(hB, non_blocking=True)
-        call_vbatch(kb, h, w, True)
+        copy_stream.wait_stream(stream)
+        with torch.cuda.stream(copy_stream):
+            w.B.copy_(hB, non_blocking=True)
+            ev_b.record(copy_stream)
+            for c in chunks:
+                a_lo, a_hi = c["a"]
+                w.A[a_lo:a_hi].copy_(hA[a_lo:a_hi], non_blocking=True)
+                c["ev"].record(copy_stream)
+        stream.wait_event(ev_b)
+        for c in chunks:
+            stream.wait_event(c["ev"])
+            st = h.call("kblasDposv_vbatch_mixed", "R", "L", c["dm"].data_ptr(), c["dn"].data_ptr(),
+                        1, c["max_n"], c["pA"].data_ptr(), c["dn"].data_ptr(), c["pB"].data_ptr(),
+                        c["dldb"].data_ptr(), c["n"], c["info"].data_ptr(), c["iter"].data_ptr())
+            if st != 1:
+                raise RuntimeError(f"kblasDposv_vbatch_mixed returned {st}")
         hX.copy_(w.B, non_blocking=True)
-        hinfo.copy_(w.info, non_blocking=True)
+        for c in chunks:
+            c["hinfo"].copy_(c["info"], non_blocking=True)
 
     t_e2e = timed_steps(torch, e2e_step, lambda: None, args.steps, args.warmup, stream)
+    torch.cuda.synchronize()
+    e2e_info = np.zeros(w.batch, dtype=np.int32)
+    for c, (lo, hi) in zip(chunks, [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]):
+        e2e_info[order[lo:hi]] = c["hinfo"].numpy()
+    xm = x_mixed.numpy()
+    e2e_check = {"info_equal": bool(np.array_equal(e2e_info, info)),
+                 "max_rel_diff_x": float(np.abs(hX.numpy() - xm).max() / np.abs(xm).max())}
     h2d = w.pool_elems * 8 + w.B0.numel() * 8
     d2h = w.B0.numel() * 8 + w.batch * 4
 
@@ -459,7 +511,9 @@ def main():
     sh = shard_mod()
     ms_mixed = sh.max_over_ranks(float(np.mean(t_mixed)))
     ms_fp64 = sh.max_over_ranks(float(np.mean(t_fp64)))
-    ms_e2e = sh.max_over_ranks(float(np.mean(t_e2e)))
+    # median step: the node's host link is shared, and single steps now and
+    # then run 2-3x slower for reasons outside this process (min/max reported)
+    ms_e2e = sh.max_over_ranks(float(np.median(t_e2e)))
     total_batch = int(sh.sum_over_ranks(w.batch))
     v_mixed = total_batch / (ms_mixed * 1e-3)
     v_fp64 = total_batch / (ms_fp64 * 1e-3)
@@ -504,7 +558,13 @@ def main():
                       "fp64_form_tflops": useful / (ms_fp64 * 1e-3) / 1e12,
                       "fp64_form_frac": useful / (ms_fp64 * 1e-3) / 1e12 / fp64_peak},
         "e2e": {"value": v_e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+                "ms_step_stats": {"median": ms_e2e, "mean": float(np.mean(t_e2e)),
+                                  "min": float(np.min(t_e2e)), "max": float(np.max(t_e2e))},
+                "host_link_gbs": h2d / (ms_e2e * 1e-3) / 1e9,
+                "pipeline": f"{len(chunks)} pieces: host->device copy of piece k+1 overlaps "
+                            f"the solve of piece k (copy stream + handle stream)",
+                "vs_resident_run": e2e_check},
         "gpu_launches": 4 * args.steps,
         "clocks": clk.summary(),
     }
