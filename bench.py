@@ -387,6 +387,243 @@ def run_reference(args):
     return 0
 
 
+# ----------------------------------------------------------------------------
+# the other configurations of the path (one JSON line each, --workload NAME)
+# ----------------------------------------------------------------------------
+def _flops_potrf(n):
+    return n ** 3 / 3.0 + n ** 2 / 2.0 + n / 6.0  # reference testing/flops.h POTRF
+
+
+def _line(metric, value, unit, ms, args, workload, extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+         "config": {"workload": workload}}
+    d.update(extra)
+    print(json.dumps(d))
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _roof(fp64_peak, flops, bytes_, ms, peaks):
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    tf = flops / (ms * 1e-3) / 1e12
+    return {"roofline": {"bound": "fp64 pipe (no FP64 tensor path on this part)",
+                         "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": tf / fp64_peak, "traffic": None,
+                         "peak_source": "FP64 FMA chains measured live in this run"},
+            "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm, "frac": gbs / hbm}}
+
+
+def run_workload(args):
+    """The configurations besides the variable-size headline."""
+    import torch
+    torch.cuda.set_device(0)
+    kb, wl = load_pkg()
+    from oracle import oracle as orc
+    orc.build()
+    stream = torch.cuda.current_stream()
+    h = kb.Handle(stream=stream.cuda_stream)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    fp64_peak = measure_fp64_peak(kb, torch)
+    rng = np.random.default_rng(1)
+    W = args.workload
+
+    if W == "potrf_potrs_n32":
+        batch, n = 10_000, 32
+        a = wl.spd_shifted(batch, n, seed=0)
+        b = wl.rhs_rows(batch, 1, n, seed=0)
+        A0, B0 = _dev(torch, a), _dev(torch, b)
+        A, B = A0.clone(), B0.clone()
+        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+
+        def step():
+            kb.check(h.call("kblasDpotrf_batch_strided", "L", n, A.data_ptr(), n, n * n, batch,
+                            info.data_ptr()), "potrf")
+            kb.check(h.call("kblasDpotrs_batch_strided", "R", "L", 1, n, A.data_ptr(), n, n * n,
+                            B.data_ptr(), 1, n, batch), "potrs")
+
+        def restore():
+            A.copy_(A0)
+            B.copy_(B0)
+
+        with ClockSampler(0) as clk:
+            t = timed_steps(torch, step, restore, args.steps, args.warmup, stream)
+        ms = float(np.median(t))
+        X = B.cpu().numpy()
+        pick = rng.choice(batch, 500, replace=False)
+        eta = orc.backward_error_r(a[pick], X[pick], b[pick], 1, n)
+        la = a[pick].copy()
+        info_ref = orc.potrf_batch(la, n)
+        flops = batch * (_flops_potrf(n) + 2.0 * n * n)
+        bytes_ = batch * (8.0 * n * (n + 1) + 16.0 * n)
+        cs = a[:2000].copy(); cb = b[:2000].copy()
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 3.0:
+            x1, y1 = cs.copy(), cb.copy()
+            orc.posv_batch(x1, y1, 1, n)
+            reps += 1
+        cpu = 2000 * reps / (time.perf_counter() - t0)
+        ex = {"fp64_gflops": flops / (ms * 1e-3) / 1e9,
+              "accuracy": {"checked": 500, "max_eta_over_10n_eps": float(eta.max() / (10 * n * EPS64)),
+                           "info_exact": bool(np.array_equal(info.cpu().numpy()[pick], info_ref))},
+              "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+              "cpu_baseline": {"value": cpu, "unit": "solves/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"2000 systems x {reps} passes"}}
+        ex.update(_roof(fp64_peak, flops, bytes_, ms, peaks))
+        ex["config"] = {"workload": "DPOTRF + DPOTRS, 10000 x n=32, strided, lda=32, 1 RHS, "
+                                    "A = G G^T + 32 I"}
+        _line("batched DPOTRF+DPOTRS solves/s (n=32)", batch / (ms * 1e-3), "solves/s", ms, args,
+              "", ex)
+        return 0
+
+    if W == "trsm_trmm_syrk_n64":
+        batch, n = 20_000, 64
+        L_ = wl.lower_tri(batch, n, seed=0, upper_fill=0.0)
+        Bm = wl.general(batch, n, n, seed=1)
+        Cs = wl.spd_shifted(batch, n, seed=2)
+        Am = wl.general(batch, n, n, seed=3)
+        dL, dB0, dC0, dA = _dev(torch, L_), _dev(torch, Bm), _dev(torch, Cs), _dev(torch, Am)
+        dB, dC = dB0.clone(), dC0.clone()
+        s2 = n * n
+        res = {}
+        for form in ("strided", "array"):
+            pL = torch.from_numpy(dL.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+            pB = torch.from_numpy(dB.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+            pA = torch.from_numpy(dA.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+            pC = torch.from_numpy(dC.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+            ops = {}
+            if form == "strided":
+                ops["trsm"] = lambda: h.call("kblasDtrsm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
+                                             dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch)
+                ops["trmm"] = lambda: h.call("kblasDtrmm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
+                                             dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch)
+                ops["syrk"] = lambda: h.call("kblasDsyrk_batch_strided", "L", "N", n, n, -1.0,
+                                             dA.data_ptr(), n, s2, 1.0, dC.data_ptr(), n, s2, batch)
+            else:
+                ops["trsm"] = lambda: h.call("kblasDtrsm_batch", "L", "L", "N", "N", n, n, 1.0,
+                                             pL.data_ptr(), n, pB.data_ptr(), n, batch)
+                ops["trmm"] = lambda: h.call("kblasDtrmm_batch", "L", "L", "N", "N", n, n, 1.0,
+                                             pL.data_ptr(), n, pB.data_ptr(), n, batch)
+                ops["syrk"] = lambda: h.call("kblasDsyrk_batch", "L", "N", n, n, -1.0,
+                                             pA.data_ptr(), n, 1.0, pC.data_ptr(), n, batch)
+            for name, fn in ops.items():
+                def call(fn=fn, name=name):
+                    kb.check(fn(), name)
+                restore = (lambda: dC.copy_(dC0)) if name == "syrk" else (lambda: dB.copy_(dB0))
+                t = timed_steps(torch, call, restore, args.steps, args.warmup, stream)
+                ms = float(np.median(t))
+                if name == "syrk":
+                    flops = batch * n * n * (n + 1.0)
+                    bytes_ = batch * (8.0 * n * n + 16.0 * n * (n + 1) / 2)
+                else:
+                    flops = batch * float(n) * n * n
+                    bytes_ = batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n)
+                res[f"{name}_{form}"] = {"ms": ms, "gflops": flops / (ms * 1e-3) / 1e9,
+                                         "gbs": bytes_ / (ms * 1e-3) / 1e9,
+                                         "fp64_frac": flops / (ms * 1e-3) / 1e12 / fp64_peak}
+        # accuracy on a sample (strided results of the last runs)
+        pick = rng.choice(batch, 200, replace=False)
+        dB.copy_(dB0)
+        kb.check(h.call("kblasDtrsm_batch_strided", "L", "L", "N", "N", n, n, 1.0, dL.data_ptr(), n,
+                        s2, dB.data_ptr(), n, s2, batch), "trsm")
+        X = dB.cpu().numpy()[pick]
+        ref = Bm[pick].copy()
+        orc.trsm_batch("L", "L", "N", "N", n, n, 1.0, L_[pick].copy(), ref)
+        trsm_err = float(np.abs(X - ref).max() / np.abs(ref).max())
+        dC.copy_(dC0)
+        kb.check(h.call("kblasDsyrk_batch_strided", "L", "N", n, n, -1.0, dA.data_ptr(), n, s2, 1.0,
+                        dC.data_ptr(), n, s2, batch), "syrk")
+        Cg = dC.cpu().numpy()[pick]
+        Cr = Cs[pick].copy()
+        orc.syrk_batch("L", "N", n, n, -1.0, Am[pick].copy(), 1.0, Cr)
+        low = np.tril(np.ones((n, n), bool)).T  # column-major lower = upper of the stored array
+        syrk_err = float(np.abs((Cg - Cr)[:, low]).max() / np.abs(Cr[:, low]).max())
+        ms = res["trsm_strided"]["ms"]
+        ex = {"ops": res, "accuracy": {"trsm_rel_err": trsm_err, "syrk_rel_err": syrk_err},
+              "gpu_launches": 6 * args.steps,
+              "config": {"workload": "DTRSM / DTRMM L,L,N,N 64x64 and DSYRK L,N 64x64, 20000 "
+                                     "matrices, strided and pointer-array"}}
+        ex.update(_roof(fp64_peak, batch * float(n) ** 3, batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n),
+                        ms, peaks))
+        _line("batched DTRSM GFLOP/s (64x64, strided; TRMM/SYRK in ops)",
+              res["trsm_strided"]["gflops"], "GFLOP/s", ms, args, "", ex)
+        return 0
+
+    if W in ("mixed_posv_n64", "posv_n512"):
+        if W == "mixed_posv_n64":
+            batch, n, m = 50_000, 64, 4
+            a, cond = wl.spd_cond(batch, n, seed=0)
+            desc = ("mixed vs FP64 DPOSV, 50000 x n=64, cond log-uniform 1e2..1e8 (Q diag Q^T), "
+                    "4 RHS, strided")
+        else:
+            batch, n, m = 2_000, 512, 8
+            a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range(batch // 100)])
+            cond = None
+            desc = ("mixed vs FP64 DPOSV, 2000 x n=512 squared-exponential covariances, "
+                    "l ~ U[0.05, 0.3], nugget 1e-4, 8 RHS, strided")
+        b = wl.rhs_rows(batch, m, n, seed=1)
+        A0, B0 = _dev(torch, a), _dev(torch, b)
+        A, B = A0.clone(), B0.clone()
+        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        it = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        kb.lib().kblas_posv_batch_mixed_wsquery(h.ptr, b"R", m, n, batch)
+        kb.lib().kblas_posv_batch_strided_wsquery(h.ptr, b"R", m, n, batch)
+        kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
+
+        def restore():
+            A.copy_(A0)
+            B.copy_(B0)
+
+        def mixed():
+            kb.check(h.call("kblasDposv_batch_mixed_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
+                            B.data_ptr(), m, m * n, batch, info.data_ptr(), it.data_ptr()), "mixed")
+
+        def fp64():
+            kb.check(h.call("kblasDposv_batch_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
+                            B.data_ptr(), m, m * n, batch, info.data_ptr()), "posv")
+
+        with ClockSampler(0) as clk:
+            tm = timed_steps(torch, mixed, restore, args.steps, args.warmup, stream)
+        Xm, itm, infom = B.cpu().numpy(), it.cpu().numpy(), info.cpu().numpy()
+        tf = timed_steps(torch, fp64, restore, max(2, args.steps // 2), 2, stream)
+        Xf, infof = B.cpu().numpy(), info.cpu().numpy()
+        ms_m, ms_f = float(np.median(tm)), float(np.median(tf))
+        ok = infof == 0
+        pick = np.where(ok)[0]
+        pick = pick[rng.choice(len(pick), min(len(pick), 400), replace=False)]
+        eta_m = orc.backward_error_r(a[pick], Xm[pick], b[pick], m, n)
+        eta_f = orc.backward_error_r(a[pick], Xf[pick], b[pick], m, n)
+        fwd = np.abs(Xm[pick] - Xf[pick]).max(axis=(1, 2)) / np.abs(Xf[pick]).max(axis=(1, 2))
+        flops = batch * (_flops_potrf(n) + 2.0 * m * n * n)
+        ex = {"fp64_form": {"value": batch / (ms_f * 1e-3), "unit": "solves/s", "ms_per_step": ms_f,
+                            "max_eta_over_10n_eps": float(eta_f.max() / (10 * n * EPS64))},
+              "mixed_over_fp64": ms_f / ms_m,
+              "accuracy": {"checked": int(len(pick)),
+                           "max_eta_over_10n_eps": float(eta_m.max() / (10 * n * EPS64)),
+                           "all_within_bound": bool((eta_m <= 10 * n * EPS64).all()),
+                           "max_forward_rel_diff_vs_fp64": float(fwd.max()),
+                           "info_equal_to_fp64_form": bool(np.array_equal(infom, infof))},
+              "refinement": {"mean_steps": float(itm[itm >= 0].mean()) if (itm >= 0).any() else None,
+                             "fallback_systems": int((itm < 0).sum())},
+              "gpu_launches": args.steps, "clocks": clk.summary(),
+              "config": {"workload": desc}}
+        ex.update(_roof(fp64_peak, flops, batch * (8.0 * n * (n + 1) + 16.0 * n * m), ms_f, peaks))
+        ex["roofline"]["note"] = "roofline of the FP64 form (the mixed form uses FP32 + FP64)"
+        _line(f"batched POSV solves/s (n={n}, {m} RHS): mixed-prec vs plain FP64",
+              batch / (ms_m * 1e-3), "solves/s", ms_m, args, "", ex)
+        return 0
+    raise SystemExit(f"unknown workload {W}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,9 +632,14 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--batch", type=int, default=100_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="vbatch",
+                    choices=["vbatch", "potrf_potrs_n32", "trsm_trmm_syrk_n64", "mixed_posv_n64",
+                             "posv_n512"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "vbatch":
+        return run_workload(args)
 
     import torch
     rank, world, local = rank_info()
