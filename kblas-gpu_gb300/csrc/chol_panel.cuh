@@ -90,6 +90,38 @@ __device__ __forceinline__ int warp_chol_rot(T (&v)[32], int jb, T tol, T *Lrow,
   return fail;
 }
 
+// The same factorization as warp_chol_rot<T, 32, CHECK_INF>, fully unrolled:
+// the column index is a compile-time constant, so row `lane` stays in place
+// (v[c] = A(lane, c)) and the updates need no register rotation and no lane
+// predicate (entries above the diagonal take harmless values that are never
+// stored or read back: every shuffle reads a lane at or below the current
+// column). About 2 (31 - c) instructions per column c, ~21 KB of code: run by
+// one warp per diagonal block, it still fits the instruction cache.
+template <typename T, bool CHECK_INF>
+__device__ __forceinline__ int warp_chol_unrolled(T (&v)[32], int jb, T tol, T *Lrow, int ldr,
+                                                  T *rinv)
+{
+  const int lane = threadIdx.x & 31;
+  int fail = 0;
+#pragma unroll
+  for (int c = 0; c < 32; c++) {
+    if (c < jb) {
+      const T d = __shfl_sync(0xffffffffu, v[c], c);
+      const bool ok = (d > tol) && (!CHECK_INF || d < T(INFINITY));
+      if (!ok && fail == 0) fail = c + 1;
+      T sq, r;
+      pivot_rs(ok ? d : T(1), sq, r);
+      const T l = (lane == c) ? sq : v[c] * r;  // L(lane, c) for lane >= c
+      v[c] = l;
+      if (lane >= c && lane < jb) Lrow[lane * ldr + c] = l;
+      if (lane == c) rinv[c] = r;
+#pragma unroll
+      for (int k = c + 1; k < 32; k++) v[k] -= l * __shfl_sync(0xffffffffu, l, k);
+    }
+  }
+  return fail;
+}
+
 // Warp-level inverse of a factored diagonal block held in the panel's
 // diagonal square (lower part, column-major, leading dimension ld a multiple
 // of 4, 16-byte aligned columns): lane j computes column j of X = L^{-1} by a
@@ -167,7 +199,7 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
       T v[32];
 #pragma unroll
       for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
-      const int f = warp_chol_rot<T, 32, CHECK_INF>(v, jb, tol, Ld, LDD, rinv + J);
+      const int f = warp_chol_unrolled<T, CHECK_INF>(v, jb, tol, Ld, LDD, rinv + J);
       __syncwarp();
       // write L_JJ back column by column (coalesced in the panel); with INV it
       // is replaced by the inverse later in this step
@@ -330,7 +362,7 @@ __device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T 
   T v[32];
 #pragma unroll
   for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
-  const int f = warp_chol_rot<T, 32, CHECK_INF>(v, jb, tol, Ldb, LDD, rinv + J);
+  const int f = warp_chol_unrolled<T, CHECK_INF>(v, jb, tol, Ldb, LDD, rinv + J);
   __syncwarp();
   for (int c = 0; c < jb; c++)
     if (lane >= c && lane < jb) Pp[lane + c * ld] = Ldb[lane * LDD + c];
