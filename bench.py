@@ -807,7 +807,9 @@ def main():
                 "pipeline": f"{len(chunks)} pieces: host->device copy of piece k+1 overlaps "
                             f"the solve of piece k (copy stream + handle stream)",
                 "vs_resident_run": e2e_check},
-        "gpu_launches": 4 * args.steps,
+        # per call: vb_count, vb_plan, vb_scatter, the panel-path and the
+        # register-path persistent kernels
+        "gpu_launches": 5 * args.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu:
