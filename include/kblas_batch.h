@@ -165,8 +165,9 @@ int kblasDposv_batch_strided(kblasHandle_t handle, char side, char uplo, const i
 
 /* Mixed-precision POSV (semantics of LAPACK DSPOSV, batched). The factor is
  * computed in FP32 after symmetric diagonal scaling; each system is refined
- * in FP64 (residual b - A*x and the update of x) until its normwise backward
- * error reaches sqrt(n)*eps64; a system whose refinement stalls, or whose
+ * in FP64 (residual b - A*x and the update of x) until its computed normwise
+ * backward error certifies a true one of at most 10*n*eps64 (computed value
+ * <= (9n-2)*eps64, eps64 = 2^-53); a system whose refinement stalls, or whose
  * FP32 factorization meets a non-positive or tiny pivot, is re-solved with
  * the FP64 factorization. iter_array (device int[batchCount], may be NULL):
  * >= 0 refinement steps taken (A is unchanged); < 0 the FP64 path was used

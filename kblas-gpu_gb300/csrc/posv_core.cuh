@@ -15,7 +15,7 @@
 //      e_i = floor(log2(a_ii)/2): exact, and keeps the FP32 factor in range;
 //   2. FP32 Cholesky As = Ls Ls^T on chip (pivot test d > n*2^-24);
 //   3. x = S Ls^-T Ls^-1 S b in FP32, then refinement: r = b - A x in FP64 (A
-//      re-read, L2 resident), stop when ||r|| <= 2 sqrt(n) eps64 (||A|| ||x|| +
+//      re-read, L2 resident), stop when ||r|| <= (9n - 2) eps64 (||A|| ||x|| +
 //      ||b||) -- with the residual's own rounding (< (n+1) eps64) this
 //      certifies a normwise backward error below 10 n eps64 -- else
 //      x += S Ls^-T Ls^-1 S r (FP32 solve, FP64 update);
@@ -41,7 +41,20 @@ constexpr int PC_NT = 256;     // threads per persistent CTA
 constexpr int PC_NCLS = 8;     // size classes (KBLAS_POSV_TUNING_CLASSES)
 constexpr int PC_MR = 4;       // right-hand sides per residual sweep (panel path)
 constexpr int PC_ITMAX = 12;   // refinement step cap
-constexpr double PC_EPS64 = 1.1102230246251565e-16;
+constexpr double PC_EPS64 = 1.1102230246251565e-16;  // 2^-53, FP64 unit roundoff
+
+// Refinement stops when the computed normwise backward error
+// eta = ||b - A x|| / (||A|| ||x|| + ||b||) (infinity norms) is at most
+// (9n - 2) u, u = 2^-53. The FP64 residual is computed with an error of at most
+// gamma_{n+1} (||b|| + ||A|| ||x||) per component, gamma_{n+1} <= (n + 1.01) u,
+// so the true backward error is then at most ((9n - 2) + (n + 1.01)) u < 10 n u,
+// the accuracy the routine guarantees; ||A|| is taken from truncated FP32 row
+// sums (never above the true norm, which only makes eta larger) or, on the
+// register path, from rounded FP32 sums inflated by at most 1 + 4e-5 (n <= 32),
+// which the 0.99 u of slack covers.
+__host__ __device__ __forceinline__ double posv_eta_target(int n) {
+  return (9.0 * n - 2.0) * PC_EPS64;
+}
 
 struct PosvCfg {
   int nmax[PC_NCLS];  // class c holds n <= nmax[c] (ascending)
@@ -230,7 +243,7 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
   const int any_bad = seg_any(bad, W);
   bool need_fb = active && (fail != 0 || any_bad);
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
-  const double tol_conv = 2.0 * sqrt((double)n) * PC_EPS64;
+  const double tol_conv = posv_eta_target(n);
   const int m_hi = warp_uniform_max_w(active ? m : 0, W);
   for (int r0 = 0; r0 < m_hi; r0++) {
     const bool go = active && !need_fb && r0 < m;
@@ -407,7 +420,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   const int any_bad = team_any(t, bad, reinterpret_cast<int *>(red));
   bool need_fb = fail != 0 || any_bad;
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
-  const double tol_conv = 2.0 * sqrt((double)n) * PC_EPS64;
+  const double tol_conv = posv_eta_target(n);
   // 3. solve + refine, PC_MR right-hand sides at a time
   for (int r0 = 0; r0 < m && !need_fb; r0 += PC_MR) {
     const int nr = min(PC_MR, m - r0);
