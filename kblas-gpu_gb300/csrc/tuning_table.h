@@ -7,27 +7,27 @@
 
 // {nmax}, {team size}, {systems per item}
 #define KGB_TUNE_MIXED_NMAX {8, 16, 32, 64, 96, 128, 176, 1024}
-#define KGB_TUNE_MIXED_TS {8, 16, 32, 32, 32, 64, 128, 256}
-#define KGB_TUNE_MIXED_SPI {32, 16, 8, 8, 8, 4, 2, 1}
+#define KGB_TUNE_MIXED_TS {8, 16, 32, 32, 64, 32, 128, 256}
+#define KGB_TUNE_MIXED_SPI {32, 16, 8, 8, 4, 8, 2, 1}
 
 #define KGB_TUNE_PLAIN_NMAX {8, 16, 32, 64, 96, 128, 176, 1024}
 #define KGB_TUNE_PLAIN_TS {8, 16, 32, 32, 32, 32, 64, 64}
 #define KGB_TUNE_PLAIN_SPI {32, 16, 8, 8, 8, 8, 4, 4}
 
 // measured ms per call, class: {team size: ms}
-//   mixed class 0: 8: 1.141, 16: 2.581, 32: 6.975
-//   mixed class 1: 16: 2.949, 32: 7.898
-//   mixed class 2: 32: 9.223
-//   mixed class 3: 32: 7.930, 64: 12.151, 128: 22.646
-//   mixed class 4: 32: 7.388, 64: 7.808, 128: 12.484, 256: 22.497
-//   mixed class 5: 32: 7.474, 64: 7.294, 128: 8.519, 256: 14.222
-//   mixed class 6: 64: 9.018, 128: 7.132, 256: 10.372
-//   mixed class 7: 64: 10.036, 128: 9.487, 256: 7.514
-//   plain class 0: 8: 0.623, 16: 1.063, 32: 2.426
-//   plain class 1: 16: 2.396, 32: 6.625
-//   plain class 2: 32: 12.186
-//   plain class 3: 32: 15.692, 64: 22.366, 128: 42.334
-//   plain class 4: 32: 14.945, 64: 19.034, 128: 30.111, 256: 56.267
-//   plain class 5: 32: 16.254, 64: 18.666, 128: 25.802, 256: 44.342
-//   plain class 6: 64: 19.945, 128: 25.175, 256: 37.459
-//   plain class 7: 64: 21.873, 128: 25.794, 256: 34.037
+//   mixed class 0: 8: 1.109, 16: 2.432, 32: 6.469
+//   mixed class 1: 16: 2.664, 32: 6.786
+//   mixed class 2: 32: 7.768
+//   mixed class 3: 32: 6.516, 64: 10.113, 128: 18.904
+//   mixed class 4: 32: 6.401, 64: 6.303, 128: 9.975, 256: 18.859
+//   mixed class 5: 32: 6.112, 64: 6.398, 128: 6.692, 256: 11.846
+//   mixed class 6: 64: 7.724, 128: 5.941, 256: 8.501
+//   mixed class 7: 64: 8.615, 128: 8.101, 256: 6.414
+//   plain class 0: 8: 0.620, 16: 1.064, 32: 2.425
+//   plain class 1: 16: 2.391, 32: 6.629
+//   plain class 2: 32: 12.191
+//   plain class 3: 32: 13.101, 64: 17.302, 128: 32.088
+//   plain class 4: 32: 13.128, 64: 15.527, 128: 23.195, 256: 43.106
+//   plain class 5: 32: 14.885, 64: 15.962, 128: 20.609, 256: 34.544
+//   plain class 6: 64: 17.927, 128: 21.214, 256: 30.100
+//   plain class 7: 64: 20.508, 128: 22.974, 256: 28.593
