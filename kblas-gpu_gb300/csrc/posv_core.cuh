@@ -71,6 +71,7 @@ __host__ __device__ __forceinline__ int pc_class(const PosvCfg &c, int n) {
 // Where the systems are: uniform strided / pointer array, or per-system arrays.
 struct SysArgs {
   int mode;  // 0 uniform strided, 1 uniform pointer array, 2 variable size
+  int op;    // plain FP64 panel path: 0 POSV (POTRF when m = 0), 2 POTRS (A holds L)
   int n, m, lda, ldb;
   double *A;
   long long sA;
@@ -87,7 +88,7 @@ struct SysArgs {
     } else {
       mm = m; la = lda; lb = ldb;
       Ap = (mode == 0) ? A + b * sA : Aarr[b];
-      Bp = (mode == 0) ? B + b * sB : Barr[b];
+      Bp = (mode == 0) ? B + b * sB : (Barr ? Barr[b] : nullptr);  // no B for POTRF
     }
   }
 };
@@ -359,6 +360,37 @@ static __device__ void panel_plain_posv(const Team &t, int n, int m, double *A, 
   int *flag = reinterpret_cast<int *>(p);
   const int inf_ = panel_fp64_posv(t, n, m, 0, A, lda, B, ldb, Ps, Ld, rinv, y, red, flag);
   if (info_out && t.tid == 0) *info_out = inf_;
+}
+
+// Plain FP64 POTRS of one team's system on the panel path: A holds the lower
+// Cholesky factor L (as POTRF leaves it); every right-hand side row of B is
+// replaced by the solution of X L L^T = B. FAC_SMEM as for panel_plain_posv.
+template <bool FAC_SMEM>
+static __device__ void panel_plain_potrs(const Team &t, int n, int m, const double *A, int lda,
+                                         double *B, int ldb, unsigned char *base,
+                                         double *Ps_scratch)
+{
+  const PanelLayout L = make_layout(n);
+  double *Ps = FAC_SMEM ? reinterpret_cast<double *>(base) : Ps_scratch;
+  unsigned char *p = base + (FAC_SMEM ? L.total() * 8 : 0);
+  p += 32 * LDD * 8;  // diagonal-block buffer of the factorization, unused here
+  double *rinv = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+  double *y = reinterpret_cast<double *>(p); p += (size_t)n * 8;
+  double *red = reinterpret_cast<double *>(p);
+  team_load_panels<double, false>(t, L, A, lda, Ps, nullptr, nullptr);
+  t.sync();
+  for (int i = t.tid; i < n; i += t.nt) {
+    const int pp = i / PNB, c = i - pp * PNB;
+    rinv[i] = 1.0 / Ps[L.base(pp) + c + (size_t)c * L.ldp(pp)];
+  }
+  t.sync();
+  for (int r0 = 0; r0 < m; r0++) {
+    for (int i = t.tid; i < n; i += t.nt) y[i] = B[(size_t)r0 + (size_t)i * ldb];
+    t.sync();
+    team_llt_solve_panel<double>(t, L, Ps, rinv, y, red, true);
+    for (int i = t.tid; i < n; i += t.nt) B[(size_t)r0 + (size_t)i * ldb] = y[i];
+    t.sync();
+  }
 }
 
 // Phase clock hooks of the mixed panel path for profiling builds; empty in
@@ -638,10 +670,16 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
         else
           panel_mixed_posv<false>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p);
       } else {
-        if (fac_smem)
+        if (sys.op == 2) {
+          if (fac_smem)
+            panel_plain_potrs<true>(t, n, m, A, lda, B, ldb, base, P64s);
+          else
+            panel_plain_potrs<false>(t, n, m, A, lda, B, ldb, base, P64s);
+        } else if (fac_smem) {
           panel_plain_posv<true>(t, n, m, A, lda, B, ldb, base, P64s, info_p);
-        else
+        } else {
           panel_plain_posv<false>(t, n, m, A, lda, B, ldb, base, P64s, info_p);
+        }
       }
       }
     }

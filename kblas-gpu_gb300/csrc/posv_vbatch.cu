@@ -112,6 +112,44 @@ size_t vbatch_ws_bytes(KBlasHandle *h, int max_n, long long batch, bool mixed) {
   return posv_ws_layout(max_n, batch, true, panel).total;
 }
 
+// Uniform FP64 POSV / POTRF / POTRS (op 0 / 1 / 2) of order n > 32 on the
+// persistent panel path: one launch, teams sized by the FP64 tuning table.
+// Returns KBLAS_InsufficientWorkspace, launching nothing, when the handle's
+// workspace is short of fp64_uniform_ws_bytes (the caller then uses the
+// one-launch blocked kernel); arguments are checked by the caller.
+size_t fp64_uniform_ws_bytes(KBlasHandle *h, int n, long long batch) {
+  if (n <= 32 || n > PC_MAX_N || batch <= 0) return 0;
+  PosvPlan pl;
+  if (plan_posv<false, 2>(h, n, pl) != KBLAS_Success) return 0;
+  return posv_ws_layout(n, batch, false, pl).total;
+}
+
+int fp64_uniform_persistent(KBlasHandle *h, int op, int m, int n, SysArgs sys, int batch,
+                            int *info) {
+  if (n <= 32 || n > PC_MAX_N) return KBLAS_NotSupported;
+  PosvPlan pl;
+  int st = plan_posv<false, 2>(h, n, pl);
+  if (st != KBLAS_Success) return st;
+  const PosvWs ws = posv_ws_layout(n, batch, false, pl);
+  if (ws.total > h->ws.allocated.d_data_bytes || !h->ws.d_data) return KBLAS_InsufficientWorkspace;
+  char *base = static_cast<char *>(h->ws.d_data);
+  int *header = reinterpret_cast<int *>(base + ws.header);
+  cudaError_t e = cudaMemsetAsync(header, 0, 64 * sizeof(int), h->stream);
+  if (e != cudaSuccess) return cuda_check(e, "cudaMemsetAsync", __FILE__, __LINE__);
+  sys.n = n;
+  sys.m = (op == 1) ? 0 : m;
+  sys.op = (op == 2) ? 2 : 0;
+  ItemArgs it{};
+  it.uniform = 1;
+  it.batch = batch;
+  it.n_uniform = n;
+  it.queue = header;
+  OutArgs out{op == 2 ? nullptr : info, nullptr, base + ws.scratch, (long long)pl.slot_bytes};
+  posv_persistent_kernel<false, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+  KGB_LAUNCH_CHECK("posv_persistent_kernel<fp64>");
+  return KBLAS_Success;
+}
+
 template <bool MIXED>
 static int vbatch(KBlasHandle *h, char side, char uplo, int *m, int *n, int max_m, int max_n,
                   double **A, int *lda, double **B, int *ldb, int batch, int *info, int *iter) {

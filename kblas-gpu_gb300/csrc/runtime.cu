@@ -226,12 +226,38 @@ void kblas_trsm_batch_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trsm_batch_strided_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trmm_batch_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trmm_batch_strided_wsquery(kblasHandle_t, char, int, int, int) {}
-void kblas_potrf_batch_wsquery(kblasHandle_t, const int, int) {}
-void kblas_potrf_batch_strided_wsquery(kblasHandle_t, const int, int) {}
-void kblas_potrs_batch_wsquery(kblasHandle_t, const int, const int, int) {}
-void kblas_potrs_batch_strided_wsquery(kblasHandle_t, const int, const int, int) {}
-void kblas_posv_batch_wsquery(kblasHandle_t, char, const int, const int, int) {}
-void kblas_posv_batch_strided_wsquery(kblasHandle_t, char, const int, const int, int) {}
+// POTRF / POTRS / POSV: the double-precision routines of order 33..1024 run
+// on the persistent panel path when this workspace is allocated (else on the
+// one-launch blocked kernel, which needs none).
+static void request_fp64_uniform(kblasHandle_t h, int n, int batch) {
+  if (!h) return;
+  KBlasWorkspaceState need;
+  need.d_data_bytes = kgb::fp64_uniform_ws_bytes(h, n, batch);
+  h->ws.requested.pad(need);
+}
+void kblas_potrf_batch_wsquery(kblasHandle_t h, const int n, int batch) { request_fp64_uniform(h, n, batch); }
+void kblas_potrf_batch_strided_wsquery(kblasHandle_t h, const int n, int batch) {
+  request_fp64_uniform(h, n, batch);
+}
+void kblas_potrs_batch_wsquery(kblasHandle_t h, const int m, const int n, int batch) {
+  (void)m;
+  request_fp64_uniform(h, n, batch);
+}
+void kblas_potrs_batch_strided_wsquery(kblasHandle_t h, const int m, const int n, int batch) {
+  (void)m;
+  request_fp64_uniform(h, n, batch);
+}
+void kblas_posv_batch_wsquery(kblasHandle_t h, char side, const int m, const int n, int batch) {
+  (void)side;
+  (void)m;
+  request_fp64_uniform(h, n, batch);
+}
+void kblas_posv_batch_strided_wsquery(kblasHandle_t h, char side, const int m, const int n,
+                                      int batch) {
+  (void)side;
+  (void)m;
+  request_fp64_uniform(h, n, batch);
+}
 
 void kblas_posv_batch_mixed_wsquery(kblasHandle_t h, char side, const int m, const int n,
                                     int batchCount) {
