@@ -602,64 +602,35 @@ __device__ void team_llt_solve_panel(const Team &t, const PanelLayout &L, const 
 }
 
 // Stage the lower triangle of A (FP64, column-major, lda) into panel storage
-// of type T. SCALE: FP32 value (float)a_ij * scl[i] * scl[j]. Padding rows and
-// the strict upper part of each diagonal block are zeroed.
-// Stage the lower triangle of A (FP64, column-major, lda) into panel storage
 // of type T (SCALE: FP32 a_ij * 2^(sh[i] + sh[j]), converted on the integer
-// pipe, see f64_to_f32_scaled; sh = -e of the row scale 2^-e). One thread per panel
-// row issues the 32 loads of the row before using any (32 loads in flight).
-// Padding rows and the strict upper part of each diagonal block get zeros.
-// rowabs (may be NULL): rowabs[i] += sum_j |a_ij| over the whole symmetric
-// row, accumulated with shared-memory atomics (row part in the thread, the
-// mirrored column part by a warp transpose-sum), for ||A||_inf.
+// pipe, see f64_to_f32_scaled; sh = -e of the row scale 2^-e). One thread per
+// panel row issues the 32 loads of the row before using any (32 loads in
+// flight). Padding rows and the strict upper part of each diagonal block get
+// zeros.
 template <typename T, bool SCALE>
 __device__ void team_load_panels(const Team &t, const PanelLayout &L, const double *__restrict__ A,
-                                 int lda, T *Ps, const int *sh, float *rowabs)
+                                 int lda, T *Ps, const int *sh)
 {
-  const int lane = t.lane();
   for (int p = 0; p < L.np; p++) {
     const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
     T *Pp = Ps + L.base(p);
-    const int rows = (ld + 31) & ~31;  // whole warps stay together for the column sums
-    for (int ii = t.tid; ii < rows; ii += t.nt) {
+    for (int ii = t.tid; ii < ld; ii += t.nt) {
       const int i = J + ii;
-      const bool in = ii < ld;        // a row of the panel (padding rows get zeros)
-      const bool real = i < L.n;      // a row of the matrix
+      const bool real = i < L.n;  // a row of the matrix (padding rows get zeros)
       const int si = (SCALE && real) ? sh[i] : 0;
-      float rsum = 0.f;
       double a[32];
 #pragma unroll
       for (int c = 0; c < 32; c++)
         a[c] = (real && c < jb && ii >= c) ? A[(size_t)i + (size_t)(J + c) * lda] : 0.0;
 #pragma unroll
-      for (int h = 0; h < 32; h += 16) {
-        float cabs[16];
-#pragma unroll
-        for (int c = 0; c < 16; c++) {
-          const float af = f64_to_f32_scaled(a[h + c], 0);
-          if (in && h + c < jb) {
-            T v;
-            if (SCALE) v = (T)f64_to_f32_scaled(a[h + c], si + sh[J + h + c]);
-            else v = (T)a[h + c];
-            Pp[ii + (h + c) * ld] = v;
-          }
-          rsum += fabsf(af);
-          cabs[c] = (ii > h + c) ? fabsf(af) : 0.f;  // strictly lower: mirrored into row J+h+c
-        }
-        if (rowabs) {
-          // column sums over the warp's 32 rows: lanes 0..15 end with columns h..h+15
-          float cs = 0.f;
-#pragma unroll
-          for (int c = 0; c < 16; c++) {
-            float v = cabs[c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == c) cs = v;
-          }
-          if (lane < 16 && h + lane < jb) atomicAdd(&rowabs[J + h + lane], cs);
+      for (int c = 0; c < 32; c++) {
+        if (c < jb) {
+          T v;
+          if (SCALE) v = (T)f64_to_f32_scaled(a[c], si + sh[J + c]);
+          else v = (T)a[c];
+          Pp[ii + c * ld] = v;
         }
       }
-      if (rowabs && real) atomicAdd(&rowabs[i], rsum);
     }
   }
 }

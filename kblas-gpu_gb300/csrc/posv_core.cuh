@@ -309,7 +309,7 @@ static __device__ int panel_fp64_posv(const Team &t, int n, int m, int r_from, d
                                double *red, int *flag)
 {
   const PanelLayout L = make_layout(n);
-  team_load_panels<double, false>(t, L, A, lda, Ps64, nullptr, nullptr);
+  team_load_panels<double, false>(t, L, A, lda, Ps64, nullptr);
   t.sync();
   const int info = team_potrf_panel<double, false>(t, L, Ps64, Ld, rinv, 0.0, flag, true);
   team_store_panels<double>(t, L, Ps64, A, lda, info ? info - 1 : n);
@@ -377,7 +377,7 @@ static __device__ void panel_plain_potrs(const Team &t, int n, int m, const doub
   double *rinv = reinterpret_cast<double *>(p); p += (size_t)n * 8;
   double *y = reinterpret_cast<double *>(p); p += (size_t)n * 8;
   double *red = reinterpret_cast<double *>(p);
-  team_load_panels<double, false>(t, L, A, lda, Ps, nullptr, nullptr);
+  team_load_panels<double, false>(t, L, A, lda, Ps, nullptr);
   t.sync();
   for (int i = t.tid; i < n; i += t.nt) {
     const int pp = i / PNB, c = i - pp * PNB;
@@ -437,7 +437,7 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   }
   t.sync();
   // 2. stage As = S A S (FP32), factor
-  team_load_panels<float, true>(t, L, A, lda, Ps, sh, nullptr);
+  team_load_panels<float, true>(t, L, A, lda, Ps, sh);
   t.sync();
   KGB_PHASE_MARK(t, 0);
   // ||A||_inf comes from the first residual (row sums of |A| on the spare
