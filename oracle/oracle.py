@@ -63,6 +63,10 @@ def lib():
                 getattr(L, f"oracle_{pfx}trmm_batch").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, Lg, P, I, Lg, I, I]
                 getattr(L, f"oracle_{pfx}syrk_batch").argtypes = [Ch, Ch, I, I, R, P, I, Lg, R, P, I, Lg, I, I]
                 getattr(L, f"oracle_{pfx}posv_vbatch").argtypes = [P, P, P, P, P, P, I, P, I]
+                getattr(L, f"oracle_{pfx}trtri_batch").argtypes = [I, I, P, I, Lg, I, P, I]
+                getattr(L, f"oracle_{pfx}lauum_batch").argtypes = [I, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}potri_batch").argtypes = [I, P, I, Lg, I, P, I]
+                getattr(L, f"oracle_{pfx}poti_batch").argtypes = [I, P, I, Lg, I, P, I]
             L.oracle_backward_error_r.argtypes = [I, I, P, I, P, I, P, I]
             L.oracle_backward_error_r.restype = D
             L.oracle_backward_error_r_batch.argtypes = [I, I, P, I, Lg, P, I, Lg, P, I, Lg, I, P, I]
@@ -181,6 +185,45 @@ def lower_rel_diff(L1: np.ndarray, L2: np.ndarray, n: int) -> float:
     L1 = np.ascontiguousarray(L1, dtype=np.float64)
     L2 = np.ascontiguousarray(L2, dtype=np.float64)
     return lib().oracle_lower_rel_diff(n, _p(L1), L1.shape[1], _p(L2), L2.shape[1])
+
+
+def trtri_batch(A: np.ndarray, n: int, unit: bool = False, nthreads=None):
+    """In-place inverse of the lower triangles of A[b] (LAPACK xTRTRI, lower);
+    returns info (first zero diagonal, 1-based; A[b] unchanged then)."""
+    assert A.flags.c_contiguous
+    batch, ncol, lda = A.shape
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"oracle_{_pfx(A)}trtri_batch")(int(unit), n, _p(A), lda, ncol * lda, batch,
+                                                   _p(info), nthreads or nthreads_default())
+    return info
+
+
+def lauum_batch(A: np.ndarray, n: int, nthreads=None):
+    """In place: lower triangle of L^T L over L (LAPACK xLAUUM, lower)."""
+    assert A.flags.c_contiguous
+    batch, ncol, lda = A.shape
+    getattr(lib(), f"oracle_{_pfx(A)}lauum_batch")(n, _p(A), lda, ncol * lda, batch,
+                                                   nthreads or nthreads_default())
+
+
+def potri_batch(A: np.ndarray, n: int, nthreads=None):
+    """In place: lower triangle of A^{-1} from the Cholesky factor in A; info."""
+    assert A.flags.c_contiguous
+    batch, ncol, lda = A.shape
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"oracle_{_pfx(A)}potri_batch")(n, _p(A), lda, ncol * lda, batch, _p(info),
+                                                   nthreads or nthreads_default())
+    return info
+
+
+def poti_batch(A: np.ndarray, n: int, nthreads=None):
+    """In place: lower triangle of A^{-1} for SPD A (POTRF + POTRI); info."""
+    assert A.flags.c_contiguous
+    batch, ncol, lda = A.shape
+    info = np.zeros(batch, dtype=np.int32)
+    getattr(lib(), f"oracle_{_pfx(A)}poti_batch")(n, _p(A), lda, ncol * lda, batch, _p(info),
+                                                  nthreads or nthreads_default())
+    return info
 
 
 def posv_vbatch(ms, ns, As, ldas, Bs, ldbs, nthreads=None):

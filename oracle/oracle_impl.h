@@ -10,8 +10,9 @@
  * test_Xtrmm_batch.cpp:330-354, test_Xsyrk_batch.cpp:380-417). LAPACK and
  * BLAS are not part of the reference tree (MKL / OpenBLAS, linked at build
  * time); this file restates the published algorithms of the reference
- * implementations of LAPACK 3.x (xPOTF2 / xPOTRS) and BLAS (xTRSM, xTRMM,
- * xSYRK) in plain C loops, with no blocking.
+ * implementations of LAPACK 3.x (xPOTF2 / xPOTRS, and for the inversion
+ * routines xTRTI2 / xLAUU2 / xPOTRI) and BLAS (xTRSM, xTRMM, xSYRK) in plain C
+ * loops, with no blocking.
  */
 
 #define ORC_CAT_(a, b) a##b
@@ -180,6 +181,76 @@ int ORC(posv)(int m, int n, REAL *A, int lda, REAL *B, int ldb)
     return info;
 }
 
+/* LAPACK xTRTRI (lower), unblocked as xTRTI2: in-place inverse of a lower
+ * triangular matrix, columns from the last: X(j,j) = 1/L(j,j), then
+ * X(j+1:n, j) = -X(j,j) * X(j+1:n, j+1:n) * L(j+1:n, j) (the trailing block
+ * already inverted, a lower triangular matrix-vector product). unit != 0: unit
+ * diagonal, not referenced. info = j (1-based) for the first L(j,j) == 0
+ * (non-unit), A then unchanged, as LAPACK xTRTRI checks before it starts. */
+int ORC(trtri)(int unit, int n, REAL *A, int lda)
+{
+    if (!unit)
+        for (int j = 0; j < n; j++)
+            if (AT(A, lda, j, j) == (REAL)0) return j + 1;
+    for (int j = n - 1; j >= 0; j--) {
+        REAL ajj;
+        if (!unit) {
+            AT(A, lda, j, j) = (REAL)1 / AT(A, lda, j, j);
+            ajj = -AT(A, lda, j, j);
+        } else {
+            ajj = (REAL)-1;
+        }
+        if (j < n - 1) {
+            /* x := X(j+1:n, j+1:n) * x, x = A(j+1:n, j), lower triangular (xTRMV) */
+            for (int i = n - 1; i > j; i--) {
+                REAL s = unit ? AT(A, lda, i, j) : AT(A, lda, i, i) * AT(A, lda, i, j);
+                for (int k = j + 1; k < i; k++) s += AT(A, lda, i, k) * AT(A, lda, k, j);
+                AT(A, lda, i, j) = s;
+            }
+            for (int i = j + 1; i < n; i++) AT(A, lda, i, j) *= ajj;
+        }
+    }
+    return 0;
+}
+
+/* LAPACK xLAUUM (lower), unblocked as xLAUU2: the lower triangle of L^T L
+ * overwrites L. Row i of the result needs rows >= i of L only, so rows are
+ * produced top-down, the diagonal entry of a row last. */
+void ORC(lauum)(int n, REAL *A, int lda)
+{
+    for (int i = 0; i < n; i++) {
+        /* B(i, j) = sum_{k >= i} L(k, i) L(k, j), j <= i */
+        for (int j = 0; j <= i; j++) {
+            REAL s = 0;
+            for (int k = i; k < n; k++) s += AT(A, lda, k, i) * AT(A, lda, k, j);
+            if (j < i) AT(A, lda, i, j) = s;
+            else {
+                /* the diagonal last: row i's other entries read L(i, i) */
+                AT(A, lda, i, i) = s;
+            }
+        }
+    }
+}
+
+/* LAPACK xPOTRI (lower): inverse of A from its Cholesky factor L (in A):
+ * xTRTRI then xLAUUM. info as xTRTRI. */
+int ORC(potri)(int n, REAL *A, int lda)
+{
+    int info = ORC(trtri)(0, n, A, lda);
+    if (info) return info;
+    ORC(lauum)(n, A, lda);
+    return 0;
+}
+
+/* POTI (the reference's kblas_poti_batch): inverse of an SPD matrix in place,
+ * xPOTRF then xPOTRI; info from the first that fails. */
+int ORC(poti)(int n, REAL *A, int lda)
+{
+    int info = ORC(potrf)(n, A, lda);
+    if (info) return info;
+    return ORC(potri)(n, A, lda);
+}
+
 /* ---------------------------- batched drivers ---------------------------- */
 /* One matrix per loop iteration, dynamic schedule, as the reference tests'
  * CPU timing loop (test_Xposv_batch.cpp:301-326). */
@@ -234,6 +305,31 @@ void ORC(syrk_batch)(char uplo, char trans, int m, int k, REAL alpha, const REAL
     for (int b = 0; b < batch; b++)
         ORC(syrk)(uplo, trans, m, k, alpha, A + (size_t)b * strideA, lda, beta,
                   C + (size_t)b * strideC, ldc);
+}
+
+void ORC(trtri_batch)(int unit, int n, REAL *A, int lda, long strideA, int batch, int *info,
+                      int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++) info[b] = ORC(trtri)(unit, n, A + (size_t)b * strideA, lda);
+}
+
+void ORC(lauum_batch)(int n, REAL *A, int lda, long strideA, int batch, int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++) ORC(lauum)(n, A + (size_t)b * strideA, lda);
+}
+
+void ORC(potri_batch)(int n, REAL *A, int lda, long strideA, int batch, int *info, int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++) info[b] = ORC(potri)(n, A + (size_t)b * strideA, lda);
+}
+
+void ORC(poti_batch)(int n, REAL *A, int lda, long strideA, int batch, int *info, int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++) info[b] = ORC(poti)(n, A + (size_t)b * strideA, lda);
 }
 
 /* Variable-size POSV over pointer arrays (host pointers here). */

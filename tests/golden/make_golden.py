@@ -103,6 +103,36 @@ def main():
                 out[key + "_A"] = a.astype(dt)
                 out[key + "_C"] = c0.astype(dt)
                 out[key + "_R"] = np.tril(res)
+    # inversion routines (own stream, so the arrays above do not change):
+    # xTRTRI / xLAUUM / xPOTRI on a Cholesky factor, and a singular TRTRI
+    r2 = rng(2025, 1)
+    for dt, name in ((np.float64, "d"), (np.float32, "s")):
+        potrf = lapack.dpotrf if name == "d" else lapack.spotrf
+        trtri, lauum, potri = ((lapack.dtrtri, lapack.dlauum, lapack.dpotri) if name == "d"
+                               else (lapack.strtri, lapack.slauum, lapack.spotri))
+        for n in (1, 2, 7, 16, 31, 33, 64, 97):
+            a = spd(n, r2).astype(dt)
+            c, info = potrf(a, lower=1, clean=1)
+            assert info == 0
+            x, info = trtri(c, lower=1, unitdiag=0)
+            assert info == 0
+            u, info = lauum(c, lower=1)
+            assert info == 0
+            pinv, info = potri(c, lower=1)
+            assert info == 0
+            key = f"{name}inv_n{n}"
+            out[key + "_A"] = a
+            out[key + "_L"] = np.tril(c)
+            out[key + "_trtri"] = np.tril(x)
+            out[key + "_lauum"] = np.tril(u)
+            out[key + "_potri"] = np.tril(pinv)
+        for n, k in ((1, 1), (9, 4), (40, 40)):
+            c = np.tril(lowtri(n, r2)).astype(dt)
+            c[k - 1, k - 1] = 0
+            x, info = trtri(c, lower=1, unitdiag=0)
+            assert info == k, (n, k, info)
+            out[f"{name}trtri_sing_n{n}_L"] = c
+            out[f"{name}trtri_sing_n{n}_info"] = np.int32(info)
     path = os.path.join(HERE, "lapack_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, len(out), "arrays", os.path.getsize(path), "bytes")

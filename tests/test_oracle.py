@@ -132,3 +132,45 @@ def test_oracle_threads_agree(orc):
     i2 = orc.potrf_batch(a2, n, nthreads=4)
     assert (i1 == 0).all() and (i2 == 0).all()
     assert np.array_equal(a1, a2)
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_inversion_vs_lapack(golden, orc, pfx):
+    """xTRTRI, xLAUUM and xPOTRI (lower) of the oracle against LAPACK, and POTI
+    (POTRF + POTRI) against LAPACK's POTRI of LAPACK's factor."""
+    dt = np.float64 if pfx == "d" else np.float32
+    ns = sorted(int(x) for x in keys(golden, rf"{pfx}inv_n(\d+)_A"))
+    assert ns, "no golden cases"
+    for n in ns:
+        L = golden[f"{pfx}inv_n{n}_L"]
+        tol = 50 * n * eps(dt)
+        for name, fn in (("trtri", orc.trtri_batch), ("lauum", orc.lauum_batch),
+                         ("potri", orc.potri_batch)):
+            ref = golden[f"{pfx}inv_n{n}_{name}"]
+            a = colmajor(L, dt)
+            info = fn(a, n, nthreads=1)
+            if info is not None:
+                assert info[0] == 0
+            got = np.tril(a[0].T)
+            rel = np.abs(got - ref).max() / np.abs(ref).max()
+            assert rel <= tol * (10 if name == "potri" else 1), (name, n, rel)
+        a = colmajor(golden[f"{pfx}inv_n{n}_A"], dt)
+        assert orc.poti_batch(a, n, nthreads=1)[0] == 0
+        ref = golden[f"{pfx}inv_n{n}_potri"]
+        rel = np.abs(np.tril(a[0].T) - ref).max() / np.abs(ref).max()
+        assert rel <= 500 * n * eps(dt), (n, rel)
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_trtri_singular_info_and_unchanged(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    ns = sorted(int(x) for x in keys(golden, rf"{pfx}trtri_sing_n(\d+)_L"))
+    assert ns
+    for n in ns:
+        L = golden[f"{pfx}trtri_sing_n{n}_L"]
+        a = colmajor(L, dt)
+        a0 = a.copy()
+        info = orc.trtri_batch(a, n, nthreads=1)
+        assert info[0] == int(golden[f"{pfx}trtri_sing_n{n}_info"])
+        assert np.array_equal(a, a0), "a singular matrix must be left unchanged"
+
