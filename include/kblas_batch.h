@@ -159,6 +159,55 @@ int kblasDposv_batch_strided(kblasHandle_t handle, char side, char uplo, const i
                              double *A, int lda, long strideA, double *B, int ldb, long strideB,
                              int batchCount, int *info_array);
 
+/* ---------------------------------------------------------------------------
+ * Inversion: TRTRI (inverse of a triangular matrix), LAUUM (L^T L), POTRI
+ * (inverse of A from its Cholesky factor L) and POTI (inverse of an SPD A),
+ * lower triangle, in place. reference include/kblas_batch.h:1611-2729.
+ * info as LAPACK: TRTRI / POTRI give the first zero diagonal entry (A then
+ * unchanged), POTI the first non-positive pivot of its Cholesky step. TRTRI
+ * also accepts diag = 'U' (the reference: non-unit only). No workspace.
+ * ------------------------------------------------------------------------- */
+void kblas_trtri_batch_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_trtri_batch_strided_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_lauum_batch_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_lauum_batch_strided_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_potri_batch_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_potri_batch_strided_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_poti_batch_wsquery(kblasHandle_t handle, const int n, int batchCount);
+void kblas_poti_batch_strided_wsquery(kblasHandle_t handle, const int n, int batchCount);
+int kblasStrtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, float **A_array,
+                      int lda, int batchCount, int *info_array);
+int kblasDtrtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, double **A_array,
+                      int lda, int batchCount, int *info_array);
+int kblasStrtri_batch_strided(kblasHandle_t handle, char uplo, char diag, const int n, float *A,
+                              int lda, long strideA, int batchCount, int *info_array);
+int kblasDtrtri_batch_strided(kblasHandle_t handle, char uplo, char diag, const int n, double *A,
+                              int lda, long strideA, int batchCount, int *info_array);
+int kblasSlauum_batch(kblasHandle_t handle, char uplo, const int n, float **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasDlauum_batch(kblasHandle_t handle, char uplo, const int n, double **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasSlauum_batch_strided(kblasHandle_t handle, char uplo, const int n, float *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasDlauum_batch_strided(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasSpotri_batch(kblasHandle_t handle, char uplo, const int n, float **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasDpotri_batch(kblasHandle_t handle, char uplo, const int n, double **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasSpotri_batch_strided(kblasHandle_t handle, char uplo, const int n, float *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasDpotri_batch_strided(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasSpoti_batch(kblasHandle_t handle, char uplo, const int n, float **A_array, int lda,
+                     int batchCount, int *info_array);
+int kblasDpoti_batch(kblasHandle_t handle, char uplo, const int n, double **A_array, int lda,
+                     int batchCount, int *info_array);
+int kblasSpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, float *A, int lda,
+                             long strideA, int batchCount, int *info_array);
+int kblasDpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
+                             long strideA, int batchCount, int *info_array);
+
 /* ===========================================================================
  * Extensions with no reference counterpart.
  * ========================================================================= */

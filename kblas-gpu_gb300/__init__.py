@@ -90,7 +90,25 @@ _SIG = {
     "kblasDposv_vbatch": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P]),
     "kblasDposv_vbatch_mixed": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P, P]),
     "kblasSetPosvTuning": (I, [I, P, P, P]),
+    "kblas_trtri_batch_wsquery": (None, [P, I, I]),
+    "kblas_trtri_batch_strided_wsquery": (None, [P, I, I]),
+    "kblas_lauum_batch_wsquery": (None, [P, I, I]),
+    "kblas_lauum_batch_strided_wsquery": (None, [P, I, I]),
+    "kblas_potri_batch_wsquery": (None, [P, I, I]),
+    "kblas_potri_batch_strided_wsquery": (None, [P, I, I]),
+    "kblas_poti_batch_wsquery": (None, [P, I, I]),
+    "kblas_poti_batch_strided_wsquery": (None, [P, I, I]),
 }
+for _x in ("S", "D"):
+    _SIG.update({
+        f"kblas{_x}trtri_batch": (I, [P, CH, CH, I, P, I, I, P]),
+        f"kblas{_x}trtri_batch_strided": (I, [P, CH, CH, I, P, I, L, I, P]),
+    })
+    for _op in ("lauum", "potri", "poti"):
+        _SIG.update({
+            f"kblas{_x}{_op}_batch": (I, [P, CH, I, P, I, I, P]),
+            f"kblas{_x}{_op}_batch_strided": (I, [P, CH, I, P, I, L, I, P]),
+        })
 for _x, _R in (("S", F), ("D", D)):
     _SIG.update({
         f"kblas{_x}syrk_batch": (I, [P, CH, CH, I, I, _R, P, I, _R, P, I, I]),
