@@ -621,6 +621,58 @@ def run_workload(args):
         _line(f"batched POSV solves/s (n={n}, {m} RHS): mixed-prec vs plain FP64",
               batch / (ms_m * 1e-3), "solves/s", ms_m, args, "", ex)
         return 0
+    if W == "inverse_n64":
+        batch, n = 20_000, 64
+        a = wl.spd_shifted(batch, n, seed=0)
+        Lh = a.copy()
+        orc.potrf_batch(Lh, n)
+        A0, L0 = _dev(torch, a), _dev(torch, Lh)
+        W_ = A0.clone()
+        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        fl = {"trtri": n ** 3 / 3.0, "lauum": n ** 3 / 3.0, "potri": 2 * n ** 3 / 3.0,
+              "poti": n ** 3}
+        res = {}
+        for op in ("trtri", "lauum", "potri", "poti"):
+            src = A0 if op == "poti" else L0
+            flags = ("L", "N") if op == "trtri" else ("L",)
+
+            def fn(op=op, flags=flags):
+                kb.check(h.call(f"kblasD{op}_batch_strided", *flags, n, W_.data_ptr(), n, n * n,
+                                batch, info.data_ptr()), op)
+            t = timed_steps(torch, fn, lambda src=src: W_.copy_(src), args.steps, args.warmup,
+                            stream)
+            ms = float(np.median(t))
+            res[op] = {"ms": ms, "gflops": batch * fl[op] / (ms * 1e-3) / 1e9,
+                       "fp64_frac": batch * fl[op] / (ms * 1e-3) / 1e12 / fp64_peak}
+        # accuracy of POTI on a sample against the oracle, CPU baseline of POTI
+        pick = rng.choice(batch, 200, replace=False)
+        W_.copy_(A0)
+        kb.check(h.call("kblasDpoti_batch_strided", "L", n, W_.data_ptr(), n, n * n, batch,
+                        info.data_ptr()), "poti")
+        got = W_.cpu().numpy()[pick]
+        ref = a[pick].copy()
+        orc.poti_batch(ref, n)
+        low = np.triu(np.ones((n, n), bool))
+        err = float(np.abs((got - ref)[:, low]).max() / np.abs(ref[:, low]).max())
+        cs = a[:2000].copy()
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 3.0:
+            x1 = cs.copy()
+            orc.poti_batch(x1, n)
+            reps += 1
+        cpu = 2000 * reps / (time.perf_counter() - t0)
+        ms = res["poti"]["ms"]
+        ex = {"ops": res, "accuracy": {"poti_rel_err_vs_oracle": err},
+              "gpu_launches": args.steps,
+              "cpu_baseline": {"value": cpu, "unit": "inverses/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"POTI, 2000 matrices x {reps} passes"},
+              "config": {"workload": "DTRTRI / DLAUUM / DPOTRI / DPOTI, 20000 x n=64, strided, "
+                                     "lower, A = G G^T + 64 I"}}
+        ex.update(_roof(fp64_peak, batch * fl["poti"], batch * 16.0 * n * (n + 1) / 2, ms, peaks))
+        _line("batched DPOTI inverses/s (n=64; TRTRI/LAUUM/POTRI in ops)", batch / (ms * 1e-3),
+              "inverses/s", ms, args, "", ex)
+        return 0
     raise SystemExit(f"unknown workload {W}")
 
 
@@ -634,7 +686,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="vbatch",
                     choices=["vbatch", "potrf_potrs_n32", "trsm_trmm_syrk_n64", "mixed_posv_n64",
-                             "posv_n512"])
+                             "posv_n512", "inverse_n64"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
