@@ -673,7 +673,148 @@ def run_workload(args):
         _line("batched DPOTI inverses/s (n=64; TRTRI/LAUUM/POTRI in ops)", batch / (ms * 1e-3),
               "inverses/s", ms, args, "", ex)
         return 0
+    if W == "gemm_vbatch":
+        return run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng)
     raise SystemExit(f"unknown workload {W}")
+
+
+def run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng):
+    """Batched DGEMM (uniform 64^3, beside cuBLAS through torch.bmm, which is
+    what the reference's uniform GEMM calls) and the variable-size DGEMM /
+    DSYRK / DTRSM, sizes uniform in 16..128, pointer arrays."""
+    res = {}
+    # uniform: 20000 x 64x64x64, C := A B + C (--batch below 20000 shrinks both
+    # parts, for profiler captures)
+    batch, n = min(20_000, args.batch), 64
+    A = torch.randn(batch, n, n, dtype=torch.float64, device="cuda")
+    B = torch.randn(batch, n, n, dtype=torch.float64, device="cuda")
+    C0 = torch.randn(batch, n, n, dtype=torch.float64, device="cuda")
+    C = C0.clone()
+    s2 = n * n
+
+    def ours():
+        kb.check(h.call("kblasDgemm_batch_strided", "N", "N", n, n, n, 1.0, A.data_ptr(), n, s2,
+                        B.data_ptr(), n, s2, 1.0, C.data_ptr(), n, s2, batch), "gemm")
+
+    def cublas():
+        # column-major C = A B + C is row-major C^T = B^T A^T + C^T: same bytes, same flops
+        C.baddbmm_(B, A)
+
+    flops_u = 2.0 * batch * n ** 3
+    for name, fn in (("dgemm_uniform_64", ours), ("cublas_bmm_uniform_64", cublas)):
+        t = timed_steps(torch, fn, lambda: C.copy_(C0), args.steps, args.warmup, stream)
+        ms = float(np.median(t))
+        res[name] = {"ms": ms, "gflops": flops_u / (ms * 1e-3) / 1e9,
+                     "fp64_frac": flops_u / (ms * 1e-3) / 1e12 / fp64_peak}
+    C.copy_(C0)
+    ours()
+    ref = torch.baddbmm(C0, B, A)
+    uni_err = float(((C - ref).abs().max() / ref.abs().max()).item())
+
+    # variable size
+    vb = min(20_000, args.batch)
+    ms_ = rng.integers(16, 129, vb).astype(np.int32)
+    ns_ = rng.integers(16, 129, vb).astype(np.int32)
+    ks_ = rng.integers(16, 129, vb).astype(np.int32)
+    mx = 128
+
+    def pool(rows, cols):
+        sizes = rows.astype(np.int64) * cols
+        offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+        buf = torch.randn(int(sizes.sum()), dtype=torch.float64, device="cuda")
+        ptrs = torch.from_numpy(buf.data_ptr() + offs * 8).cuda()
+        return buf, ptrs, offs
+
+    Ab, pA, oA = pool(ms_, ks_)
+    Bb, pB, oB = pool(ks_, ns_)
+    Cb0, pC, oC = pool(ms_, ns_)
+    Cb = Cb0.clone()
+    pC = torch.from_numpy(Cb.data_ptr() + oC * 8).cuda()
+    dm, dn, dk = (torch.from_numpy(v).cuda() for v in (ms_, ns_, ks_))
+
+    def vgemm():
+        kb.check(h.call("kblasDgemm_vbatch", "N", "N", dm.data_ptr(), dn.data_ptr(), dk.data_ptr(),
+                        mx, mx, mx, 1.0, pA.data_ptr(), dm.data_ptr(), pB.data_ptr(),
+                        dk.data_ptr(), 1.0, pC.data_ptr(), dm.data_ptr(), vb), "gemm_vbatch")
+
+    # SYRK: C_i (m_i x m_i) := -A_i A_i^T + C_i with A_i = the m_i x k_i GEMM operand;
+    # TRSM: L_i X = B, L_i the leading m_i x m_i block of C_i made well conditioned
+    Sb0, pS, oS = pool(ms_, ms_)
+    Sb = Sb0.clone()
+    pS = torch.from_numpy(Sb.data_ptr() + oS * 8).cuda()
+    Lb = Sb0.clone()
+    # diagonally dominant lower triangles: scale the pool, then add 2 on the diagonals
+    Lb.mul_(0.1)
+    diag_idx = np.concatenate([o + np.arange(m) * (m + 1) for o, m in zip(oS, ms_)])
+    Lb[torch.from_numpy(diag_idx).cuda()] += 2.0
+    pL = torch.from_numpy(Lb.data_ptr() + oS * 8).cuda()
+    Xb0, pX, oX = pool(ms_, ns_)
+    Xb = Xb0.clone()
+    pX = torch.from_numpy(Xb.data_ptr() + oX * 8).cuda()
+
+    def vsyrk():
+        kb.check(h.call("kblasDsyrk_vbatch", "L", "N", dm.data_ptr(), dk.data_ptr(), mx, mx, -1.0,
+                        pA.data_ptr(), dm.data_ptr(), 1.0, pS.data_ptr(), dm.data_ptr(), vb),
+                 "syrk_vbatch")
+
+    def vtrsm():
+        kb.check(h.call("kblasDtrsm_vbatch", "L", "L", "N", "N", dm.data_ptr(), dn.data_ptr(), mx,
+                        mx, 1.0, pL.data_ptr(), dm.data_ptr(), pX.data_ptr(), dm.data_ptr(), vb),
+                 "trsm_vbatch")
+
+    fl = {"dgemm_vbatch": float(2.0 * (ms_.astype(np.float64) * ns_ * ks_).sum()),
+          "dsyrk_vbatch": float((ms_.astype(np.float64) * (ms_ + 1) * ks_).sum()),
+          "dtrsm_vbatch": float((ms_.astype(np.float64) ** 2 * ns_).sum())}
+    with ClockSampler(0) as clk:
+        for name, fn, rst in (("dgemm_vbatch", vgemm, lambda: Cb.copy_(Cb0)),
+                              ("dsyrk_vbatch", vsyrk, lambda: Sb.copy_(Sb0)),
+                              ("dtrsm_vbatch", vtrsm, lambda: Xb.copy_(Xb0))):
+            t = timed_steps(torch, fn, rst, args.steps, args.warmup, stream)
+            ms = float(np.median(t))
+            res[name] = {"ms": ms, "gflops": fl[name] / (ms * 1e-3) / 1e9,
+                         "fp64_frac": fl[name] / (ms * 1e-3) / 1e12 / fp64_peak}
+    # accuracy of the variable-size GEMM on a sample against the oracle
+    Cb.copy_(Cb0)
+    vgemm()
+    Ch, Ah, Bh, C0h = Cb.cpu().numpy(), Ab.cpu().numpy(), Bb.cpu().numpy(), Cb0.cpu().numpy()
+    worst = 0.0
+    for i in rng.choice(vb, 100, replace=False):
+        m, nn, k = int(ms_[i]), int(ns_[i]), int(ks_[i])
+        a = Ah[oA[i]:oA[i] + m * k].reshape(1, k, m).copy()
+        b = Bh[oB[i]:oB[i] + k * nn].reshape(1, nn, k).copy()
+        c = C0h[oC[i]:oC[i] + m * nn].reshape(1, nn, m).copy()
+        orc.gemm_batch("N", "N", m, nn, k, 1.0, a, b, 1.0, c, nthreads=1)
+        got = Ch[oC[i]:oC[i] + m * nn].reshape(1, nn, m)
+        worst = max(worst, float(np.abs(got - c).max() / np.abs(c).max()))
+    # CPU baseline: the oracle's DGEMM over a sample of the variable-size batch
+    sample = rng.choice(vb, 400, replace=False)
+    t0 = time.perf_counter()
+    done_fl = 0.0
+    while time.perf_counter() - t0 < 3.0:
+        for i in sample[:40]:
+            m, nn, k = int(ms_[i]), int(ns_[i]), int(ks_[i])
+            a = Ah[oA[i]:oA[i] + m * k].reshape(1, k, m)
+            b = Bh[oB[i]:oB[i] + k * nn].reshape(1, nn, k)
+            c = C0h[oC[i]:oC[i] + m * nn].reshape(1, nn, m).copy()
+            orc.gemm_batch("N", "N", m, nn, k, 1.0, a, b, 1.0, c, nthreads=1)
+            done_fl += 2.0 * m * nn * k
+    cpu_gf = done_fl / (time.perf_counter() - t0) / 1e9
+    ms = res["dgemm_vbatch"]["ms"]
+    ex = {"ops": res,
+          "accuracy": {"uniform_rel_err_vs_cublas": uni_err, "vbatch_rel_err_vs_oracle": worst},
+          "gpu_launches": 5 * args.steps, "clocks": clk.summary(),
+          "cpu_baseline": {"value": cpu_gf, "unit": "GFLOP/s", "cores": 1, "kind": "port",
+                           "sample": "oracle DGEMM (scalar C loops) on 40 of the variable-size "
+                                     "products, repeated for 3 s, one thread"},
+          "config": {"workload": f"DGEMM N,N: uniform {batch} x 64^3 strided (and cuBLAS via "
+                                 f"torch.baddbmm beside it); variable-size DGEMM / DSYRK L,N / "
+                                 f"DTRSM L,L,N,N over {vb} matrices, m, n, k uniform in 16..128, "
+                                 f"pointer arrays, sizes in device arrays"}}
+    bytes_ = 8.0 * float((ms_.astype(np.float64) * ks_ + ks_ * ns_ + 2.0 * ms_ * ns_).sum())
+    ex.update(_roof(fp64_peak, fl["dgemm_vbatch"], bytes_, ms, peaks))
+    _line("variable-size batched DGEMM GFLOP/s (m, n, k in 16..128)", res["dgemm_vbatch"]["gflops"],
+          "GFLOP/s", ms, args, "", ex)
+    return 0
 
 
 def main():
@@ -686,7 +827,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="vbatch",
                     choices=["vbatch", "potrf_potrs_n32", "trsm_trmm_syrk_n64", "mixed_posv_n64",
-                             "posv_n512", "inverse_n64"])
+                             "posv_n512", "inverse_n64", "gemm_vbatch"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

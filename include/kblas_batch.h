@@ -17,9 +17,10 @@
  *  - info arrays are device int[batchCount]; 0 = success, +j = the leading
  *    minor of order j is not positive definite (LAPACK xPOTRF semantics, the
  *    meaning documented at reference include/kblas_batch.h:1482);
- *  - flag combinations the reference leaves unimplemented (Upper factor,
- *    POTRS/POSV with side = Left) return KBLAS_NotImplemented like the
- *    reference; TRSM/TRMM additionally implement Upper, Unit and Right, which
+ *  - flag combinations the reference leaves unimplemented (it returns
+ *    KBLAS_NotImplemented) run here: Upper POTRF / POTRS / POSV / SYRK /
+ *    TRTRI / LAUUM / POTRI / POTI and side 'L' POTRS / POSV; TRSM/TRMM
+ *    implement Upper, Unit and Right natively, which
  *    the reference only reaches through MAGMA.
  */
 #ifndef KBLAS_GB300_BATCH_H
@@ -55,10 +56,10 @@ void kblas_posv_batch_wsquery(kblasHandle_t handle, char side, const int m, cons
 void kblas_posv_batch_strided_wsquery(kblasHandle_t handle, char side, const int m, const int n, int batchCount);
 
 /* ---------------------------------------------------------------------------
- * SYRK: B := alpha*op(A)*op(A)^T + beta*B on the lower triangle of B (m x m);
+ * SYRK: B := alpha*op(A)*op(A)^T + beta*B on the uplo triangle of B (m x m);
  * op(A) is m x n (trans = 'N') or A is n x m (trans = 'T').
- * reference include/kblas_batch.h:631-728 (uplo = 'U' -> KBLAS_NotImplemented,
- * as reference src/batch_triangular/Xsyrk_batch_drivers.cuh:133-136).
+ * reference include/kblas_batch.h:631-728 (uplo = 'U' is KBLAS_NotImplemented
+ * there, src/batch_triangular/Xsyrk_batch_drivers.cuh:133-136; supported here).
  * ------------------------------------------------------------------------- */
 int kblasSsyrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
                      const float alpha, const float **A_array, int lda,
@@ -113,8 +114,9 @@ int kblasDtrmm_batch_strided(kblasHandle_t handle, char side, char uplo, char tr
                              double *B, int ldb, long strideB, int batchCount);
 
 /* ---------------------------------------------------------------------------
- * POTRF: A = L*L^T in place (lower triangle only; the strict upper triangle
- * is neither read nor written). reference include/kblas_batch.h:1486-1566.
+ * POTRF: A = L*L^T (uplo 'L') or A = U^T*U (uplo 'U', KBLAS_NotImplemented in
+ * the reference) in place; only the uplo triangle is read and written.
+ * reference include/kblas_batch.h:1486-1566.
  * ------------------------------------------------------------------------- */
 int kblasSpotrf_batch(kblasHandle_t handle, char uplo, const int n,
                       float **A_array, int lda, int batchCount, int *info_array);
@@ -126,9 +128,10 @@ int kblasDpotrf_batch_strided(kblasHandle_t handle, char uplo, const int n,
                               double *A, int lda, long strideA, int batchCount, int *info_array);
 
 /* ---------------------------------------------------------------------------
- * POTRS: solve X*A = B with A = L*L^T given by its factor L (side 'R',
- * uplo 'L'); B is m x n (m right-hand sides stored as rows) and is
- * overwritten by X. reference include/kblas_batch.h:2190-2278.
+ * POTRS: solve X*A = B (side 'R', A n x n) or A*X = B (side 'L', A m x m)
+ * with A = L*L^T or U^T*U given by its factor (uplo 'L' / 'U'); B is m x n
+ * and is overwritten by X. reference include/kblas_batch.h:2190-2278 (side
+ * 'R' + uplo 'L' only there; the other three run as two TRSM passes here).
  * ------------------------------------------------------------------------- */
 int kblasSpotrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
                       const float **A_array, int lda, float **B_array, int ldb, int batchCount);
@@ -142,9 +145,10 @@ int kblasDpotrs_batch_strided(kblasHandle_t handle, char side, char uplo, const 
                               double *B, int ldb, long strideB, int batchCount);
 
 /* ---------------------------------------------------------------------------
- * POSV: POTRF then POTRS, fused into one kernel per size class. On exit A
- * holds L and B holds X; for a matrix with info > 0, B is left unchanged
- * (LAPACK xPOSV). reference include/kblas_batch.h:2896-2988.
+ * POSV: POTRF then POTRS, fused into one kernel per size class for side 'R'
+ * (either uplo); side 'L' factors, then solves with two TRSM passes. On exit A
+ * holds the factor and B holds X; for a matrix with info > 0, B is left
+ * unchanged (LAPACK xPOSV). reference include/kblas_batch.h:2896-2988.
  * ------------------------------------------------------------------------- */
 int kblasSposv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
                      float **A_array, int lda, float **B_array, int ldb,
@@ -160,9 +164,9 @@ int kblasDposv_batch_strided(kblasHandle_t handle, char side, char uplo, const i
                              int batchCount, int *info_array);
 
 /* ---------------------------------------------------------------------------
- * Inversion: TRTRI (inverse of a triangular matrix), LAUUM (L^T L), POTRI
- * (inverse of A from its Cholesky factor L) and POTI (inverse of an SPD A),
- * lower triangle, in place. reference include/kblas_batch.h:1611-2729.
+ * Inversion: TRTRI (inverse of a triangular matrix), LAUUM (L^T L or U U^T),
+ * POTRI (inverse of A from its Cholesky factor) and POTI (inverse of an SPD
+ * A), either triangle (the reference: lower only), in place. reference include/kblas_batch.h:1611-2729.
  * info as LAPACK: TRTRI / POTRI give the first zero diagonal entry (A then
  * unchanged), POTI the first non-positive pivot of its Cholesky step. TRTRI
  * also accepts diag = 'U' (the reference: non-unit only). No workspace.
@@ -208,6 +212,67 @@ int kblasSpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, float
 int kblasDpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
                              long strideA, int batchCount, int *info_array);
 
+/* ---------------------------------------------------------------------------
+ * GEMM: C := alpha*op(A)*op(B) + beta*C, op(A) m x k, op(B) k x n.
+ * reference include/kblas_batch.h:35-36 (wsqueries), :309-460 (C names;
+ * cuBLAS there, a native tile kernel here). batchCount < 1 ->
+ * KBLAS_Error_WrongInput, as the reference. No workspace.
+ * ------------------------------------------------------------------------- */
+void kblas_gemm_batch_strided_wsquery(kblasHandle_t handle, int batchCount);
+void kblas_gemm_batch_nonuniform_wsquery(kblasHandle_t handle);
+int kblasSgemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const float alpha, const float **A, int lda, const float **B,
+                     int ldb, const float beta, float **C, int ldc, int batchCount);
+int kblasDgemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const double alpha, const double **A, int lda,
+                     const double **B, int ldb, const double beta, double **C, int ldc,
+                     int batchCount);
+int kblasSgemm_batch_strided(kblasHandle_t handle, char transA, char transB, const int m,
+                             const int n, const int k, const float alpha, const float *A, int lda,
+                             long strideA, const float *B, int ldb, long strideB, const float beta,
+                             float *C, int ldc, long strideC, int batchCount);
+int kblasDgemm_batch_strided(kblasHandle_t handle, char transA, char transB, const int m,
+                             const int n, const int k, const double alpha, const double *A,
+                             int lda, long strideA, const double *B, int ldb, long strideB,
+                             const double beta, double *C, int ldc, long strideC, int batchCount);
+
+/* ---------------------------------------------------------------------------
+ * Variable-size GEMM / SYRK / TRSM. The reference has these as C++ overloads
+ * of kblas_{gemm,syrk,trsm}_batch taking per-matrix sizes and leading
+ * dimensions in DEVICE int arrays (include/kblas_batch.h:201-245, :524-550,
+ * :829-860; MAGMA-only there); these are their C names, and the overloads
+ * below forward to them. max_* are host-side upper bounds of the sizes; all
+ * of them <= 0 means "unknown". GEMM and SYRK need no bound (it only sizes
+ * the grid) and no workspace. TRSM sizes its shared-memory layout from the
+ * bound: when max_m and max_n are both <= 0 it recomputes them on the device
+ * into the workspace kblas_trsm_batch_nonuniform_wsquery requests, and
+ * synchronises the stream (as the reference). Per-matrix sizes are not
+ * validated; matrices with a size <= 0 are skipped. SYRK accepts uplo 'L'
+ * and 'U'; TRSM every side / uplo / trans / diag.
+ * ------------------------------------------------------------------------- */
+void kblas_syrk_batch_nonuniform_wsquery(kblasHandle_t handle);
+void kblas_trsm_batch_nonuniform_wsquery(kblasHandle_t handle);
+int kblasSgemm_vbatch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                      int max_m, int max_n, int max_k, const float alpha, const float **A,
+                      int *lda, const float **B, int *ldb, const float beta, float **C, int *ldc,
+                      int batchCount);
+int kblasDgemm_vbatch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                      int max_m, int max_n, int max_k, const double alpha, const double **A,
+                      int *lda, const double **B, int *ldb, const double beta, double **C,
+                      int *ldc, int batchCount);
+int kblasSsyrk_vbatch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                      int max_n, const float alpha, const float **A, int *lda, const float beta,
+                      float **B, int *ldb, int batchCount);
+int kblasDsyrk_vbatch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                      int max_n, const double alpha, const double **A, int *lda,
+                      const double beta, double **B, int *ldb, int batchCount);
+int kblasStrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                      int *n, int max_m, int max_n, const float alpha, const float **A, int *lda,
+                      float **B, int *ldb, int batchCount);
+int kblasDtrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                      int *n, int max_m, int max_n, const double alpha, const double **A,
+                      int *lda, double **B, int *ldb, int batchCount);
+
 /* ===========================================================================
  * Extensions with no reference counterpart.
  * ========================================================================= */
@@ -220,7 +285,9 @@ int kblasDpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, doubl
  * FP32 factorization meets a non-positive or tiny pivot, is re-solved with
  * the FP64 factorization. iter_array (device int[batchCount], may be NULL):
  * >= 0 refinement steps taken (A is unchanged); < 0 the FP64 path was used
- * (A holds L): -1 FP32 pivot test failed, -2 refinement stalled, -3 step cap.
+ * (A holds L): -1 FP32 pivot test failed, -2 refinement stalled (error not
+ * halved by a step, or contracting too slowly for the remaining steps to cost
+ * less than the FP64 factorization), -3 step cap.
  * info_array as for POSV. Needs workspace: kblas_posv_batch_mixed_wsquery. */
 void kblas_posv_batch_mixed_wsquery(kblasHandle_t handle, char side, const int m, const int n,
                                     int batchCount);
@@ -356,6 +423,41 @@ int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, c
 int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
                      const double alpha, const double *A, int lda, long strideA,
                      const double beta, double *B, int ldb, long strideB, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const float alpha, const float **A, int lda, const float **B,
+                     int ldb, const float beta, float **C, int ldc, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const double alpha, const double **A, int lda,
+                     const double **B, int ldb, const double beta, double **C, int ldc,
+                     int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const float alpha, const float *A, int lda, long strideA,
+                     const float *B, int ldb, long strideB, const float beta, float *C, int ldc,
+                     long strideC, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const double alpha, const double *A, int lda, long strideA,
+                     const double *B, int ldb, long strideB, const double beta, double *C,
+                     int ldc, long strideC, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const float alpha, const float **A,
+                     int *lda, const float **B, int *ldb, const float beta, float **C, int *ldc,
+                     int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const double alpha, const double **A,
+                     int *lda, const double **B, int *ldb, const double beta, double **C,
+                     int *ldc, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                     int max_n, float alpha, float **A, int *lda, float beta, float **B, int *ldb,
+                     int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                     int max_n, double alpha, double **A, int *lda, double beta, double **B,
+                     int *ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                     int *n, int max_m, int max_n, float alpha, float **A, int *lda, float **B,
+                     int *ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                     int *n, int max_m, int max_n, double alpha, double **A, int *lda,
+                     double **B, int *ldb, int batchCount);
 #endif /* __cplusplus */
 
 #endif /* KBLAS_GB300_BATCH_H */

@@ -98,6 +98,10 @@ _SIG = {
     "kblas_potri_batch_strided_wsquery": (None, [P, I, I]),
     "kblas_poti_batch_wsquery": (None, [P, I, I]),
     "kblas_poti_batch_strided_wsquery": (None, [P, I, I]),
+    "kblas_gemm_batch_strided_wsquery": (None, [P, I]),
+    "kblas_gemm_batch_nonuniform_wsquery": (None, [P]),
+    "kblas_syrk_batch_nonuniform_wsquery": (None, [P]),
+    "kblas_trsm_batch_nonuniform_wsquery": (None, [P]),
 }
 for _x in ("S", "D"):
     _SIG.update({
@@ -123,6 +127,12 @@ for _x, _R in (("S", F), ("D", D)):
         f"kblas{_x}potrs_batch_strided": (I, [P, CH, CH, I, I, P, I, L, P, I, L, I]),
         f"kblas{_x}posv_batch": (I, [P, CH, CH, I, I, P, I, P, I, I, P]),
         f"kblas{_x}posv_batch_strided": (I, [P, CH, CH, I, I, P, I, L, P, I, L, I, P]),
+        f"kblas{_x}gemm_batch": (I, [P, CH, CH, I, I, I, _R, P, I, P, I, _R, P, I, I]),
+        f"kblas{_x}gemm_batch_strided": (I, [P, CH, CH, I, I, I, _R, P, I, L, P, I, L, _R, P, I,
+                                             L, I]),
+        f"kblas{_x}gemm_vbatch": (I, [P, CH, CH, P, P, P, I, I, I, _R, P, P, P, P, _R, P, P, I]),
+        f"kblas{_x}syrk_vbatch": (I, [P, CH, CH, P, P, I, I, _R, P, P, _R, P, P, I]),
+        f"kblas{_x}trsm_vbatch": (I, [P, CH, CH, CH, CH, P, P, I, I, _R, P, P, P, P, I]),
     })
 
 EXPORTED = sorted(_SIG)

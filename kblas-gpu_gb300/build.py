@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", INC, "-I", CSRC] + ARCH
 
-LIB_UNITS = ["runtime.cu", "potrf_posv.cu", "trsm_trmm.cu", "syrk.cu", "inverse.cu", "posv_mixed.cu",
+LIB_UNITS = ["runtime.cu", "potrf_posv.cu", "trsm_trmm.cu", "syrk.cu", "gemm_batch.cu", "inverse.cu", "posv_mixed.cu",
              "posv_vbatch.cu", "posv_noalloc.cu", "cxx_overloads.cu"]
 PROBE_UNITS = ["probe.cu"]
 

@@ -128,3 +128,73 @@ int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const 
   return kblasDsyrk_batch_strided(h, uplo, trans, m, n, alpha, A, lda, strideA, beta, B, ldb, strideB,
                                   batchCount);
 }
+
+// GEMM, reference include/kblas_batch.h:82-190 (uniform) and :201-245
+// (variable-size).
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, const int m, const int n,
+                     const int k, const float alpha, const float **A, int lda, const float **B,
+                     int ldb, const float beta, float **C, int ldc, int batchCount) {
+  return kblasSgemm_batch(h, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                          batchCount);
+}
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, const int m, const int n,
+                     const int k, const double alpha, const double **A, int lda, const double **B,
+                     int ldb, const double beta, double **C, int ldc, int batchCount) {
+  return kblasDgemm_batch(h, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                          batchCount);
+}
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, const int m, const int n,
+                     const int k, const float alpha, const float *A, int lda, long strideA,
+                     const float *B, int ldb, long strideB, const float beta, float *C, int ldc,
+                     long strideC, int batchCount) {
+  return kblasSgemm_batch_strided(h, transA, transB, m, n, k, alpha, A, lda, strideA, B, ldb,
+                                  strideB, beta, C, ldc, strideC, batchCount);
+}
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, const int m, const int n,
+                     const int k, const double alpha, const double *A, int lda, long strideA,
+                     const double *B, int ldb, long strideB, const double beta, double *C,
+                     int ldc, long strideC, int batchCount) {
+  return kblasDgemm_batch_strided(h, transA, transB, m, n, k, alpha, A, lda, strideA, B, ldb,
+                                  strideB, beta, C, ldc, strideC, batchCount);
+}
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const float alpha, const float **A,
+                     int *lda, const float **B, int *ldb, const float beta, float **C, int *ldc,
+                     int batchCount) {
+  return kblasSgemm_vbatch(h, transA, transB, m, n, k, max_m, max_n, max_k, alpha, A, lda, B, ldb,
+                           beta, C, ldc, batchCount);
+}
+int kblas_gemm_batch(kblasHandle_t h, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const double alpha, const double **A,
+                     int *lda, const double **B, int *ldb, const double beta, double **C,
+                     int *ldc, int batchCount) {
+  return kblasDgemm_vbatch(h, transA, transB, m, n, k, max_m, max_n, max_k, alpha, A, lda, B, ldb,
+                           beta, C, ldc, batchCount);
+}
+
+// Variable-size SYRK and TRSM, reference include/kblas_batch.h:524-550 and
+// :829-860.
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     float alpha, float **A, int *lda, float beta, float **B, int *ldb,
+                     int batchCount) {
+  return kblasSsyrk_vbatch(h, uplo, trans, m, n, max_m, max_n, alpha, (const float **)A, lda, beta,
+                           B, ldb, batchCount);
+}
+int kblas_syrk_batch(kblasHandle_t h, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     double alpha, double **A, int *lda, double beta, double **B, int *ldb,
+                     int batchCount) {
+  return kblasDsyrk_vbatch(h, uplo, trans, m, n, max_m, max_n, alpha, (const double **)A, lda,
+                           beta, B, ldb, batchCount);
+}
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, float alpha, float **A, int *lda, float **B, int *ldb,
+                     int batchCount) {
+  return kblasStrsm_vbatch(h, side, uplo, trans, diag, m, n, max_m, max_n, alpha,
+                           (const float **)A, lda, B, ldb, batchCount);
+}
+int kblas_trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, double alpha, double **A, int *lda, double **B,
+                     int *ldb, int batchCount) {
+  return kblasDtrsm_vbatch(h, side, uplo, trans, diag, m, n, max_m, max_n, alpha,
+                           (const double **)A, lda, B, ldb, batchCount);
+}

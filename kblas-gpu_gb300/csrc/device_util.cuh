@@ -22,6 +22,25 @@ struct PtrArr {
   __device__ __forceinline__ T *get(long long b) const { return arr[b]; }
 };
 
+// Per-matrix integer arguments: N values shared by all matrices, or N device
+// arrays read at the matrix index.
+template <int N>
+struct DimsU {
+  int v[N];
+  __device__ __forceinline__ void get(long long, int (&o)[N]) const {
+#pragma unroll
+    for (int i = 0; i < N; i++) o[i] = v[i];
+  }
+};
+template <int N>
+struct DimsV {
+  const int *p[N];
+  __device__ __forceinline__ void get(long long b, int (&o)[N]) const {
+#pragma unroll
+    for (int i = 0; i < N; i++) o[i] = p[i][b];
+  }
+};
+
 // 1/sqrt(d) and sqrt(d) for a positive pivot d: one reciprocal square root
 // (CUDA's rsqrt / rsqrtf) and one multiply, instead of a square root and a
 // division per column.

@@ -1,11 +1,12 @@
-// inverse.cu -- batched TRTRI / LAUUM / POTRI / POTI (lower), single and
+// inverse.cu -- batched TRTRI / LAUUM / POTRI / POTI, single and
 // double precision, strided and pointer-array forms.
 //
 // Entry points replace reference src/batch_triangular/Xtrtri_batch.cu:86,
 // Xlauum_batch.cu:86, Xpotri_batch.cu:86 and Xpoti_batch.cu:86 (names and
-// arguments of include/kblas_batch.h:1611-2729). Like the reference, Upper
-// returns KBLAS_NotImplemented; TRTRI also takes a unit diagonal (a superset:
-// the reference supports non-unit only). info follows LAPACK: TRTRI / POTRI
+// arguments of include/kblas_batch.h:1611-2729). The reference returns
+// KBLAS_NotImplemented for Upper; here Upper runs the lower kernel between two
+// in-place transposes. TRTRI also takes a unit diagonal (a superset: the
+// reference supports non-unit only). info follows LAPACK: TRTRI / POTRI
 // report the first zero diagonal entry of the triangle (1-based) and leave A
 // unchanged; POTI reports the first non-positive pivot of its Cholesky step and
 // leaves A as LAPACK xPOTRF does.
@@ -23,6 +24,7 @@
 #include "device_util.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
+#include "uplo_swap.cuh"
 
 namespace kgb {
 
@@ -172,12 +174,9 @@ __global__ void __launch_bounds__(256) inverse_kernel(int n, Acc A, int lda, lon
 // uplo tests of the LAUUM / POTRI / POTI drivers)
 static int check_inverse(KBlasHandle *h, char uplo, char diag, bool has_diag, int n, int lda,
                          int batch, const void *A, const char *name) {
+  (void)name;
   if (!h) return KBLAS_Error_NotInitialized;
-  if (is_upper(uplo)) {
-    printf("Upper %s_BATCH is not implemented yet\n", name);
-    return KBLAS_NotImplemented;
-  }
-  if (!is_lower(uplo)) return KBLAS_Error_WrongInput;
+  if (!is_lower(uplo) && !is_upper(uplo)) return KBLAS_Error_WrongInput;
   if (has_diag && !is_unit(diag) && !is_nonunit(diag)) return KBLAS_Error_WrongInput;
   if (n < 0 || batch < 0 || lda < (n > 1 ? n : 1)) return KBLAS_Error_WrongInput;
   if (n > 0 && batch > 0 && !A) return KBLAS_Error_WrongInput;
@@ -204,14 +203,30 @@ static int launch_inverse(KBlasHandle *h, int n, Acc A, int lda, int batch, int 
   return KBLAS_Success;
 }
 
+// uplo 'U': the lower kernel between two in-place transposes (uplo_swap.cuh):
+// the upper factor U is L^T of A^T, inv(U) = inv(L)^T, U U^T = (L^T L)^T
+// stored as its upper triangle, inv(A) likewise.
+template <typename T, int OP, class Acc>
+static int launch_inverse_uplo(KBlasHandle *h, bool upper, int n, Acc A, int lda, int batch,
+                               int *info, bool unit) {
+  if (!upper || n <= 1 || batch == 0)
+    return launch_inverse<T, OP>(h, n, A, lda, batch, info, unit);
+  if (n > INV_MAX_N) return KBLAS_NotSupported;
+  int st = swap_uplo<T>(h, n, A, lda, batch);
+  if (st != KBLAS_Success) return st;
+  st = launch_inverse<T, OP>(h, n, A, lda, batch, info, unit);
+  const int st2 = swap_uplo<T>(h, n, A, lda, batch);
+  return st != KBLAS_Success ? st : st2;
+}
+
 template <typename T, int OP>
 static int inv_strided(KBlasHandle *h, char uplo, char diag, int n, T *A, int lda, long long sA,
                        int batch, int *info, const char *name) {
   int st = check_inverse(h, uplo, diag, OP == INV_TRTRI, n, lda, batch, A, name);
   if (st != KBLAS_Success) return st;
   if (batch > 1 && sA < (long long)lda * n) return KBLAS_Error_WrongInput;
-  return launch_inverse<T, OP>(h, n, Strided<T>{A, sA}, lda, batch, info,
-                               OP == INV_TRTRI && is_unit(diag));
+  return launch_inverse_uplo<T, OP>(h, is_upper(uplo), n, Strided<T>{A, sA}, lda, batch, info,
+                                    OP == INV_TRTRI && is_unit(diag));
 }
 
 template <typename T, int OP>
@@ -219,8 +234,8 @@ static int inv_array(KBlasHandle *h, char uplo, char diag, int n, T **A, int lda
                      int *info, const char *name) {
   int st = check_inverse(h, uplo, diag, OP == INV_TRTRI, n, lda, batch, A, name);
   if (st != KBLAS_Success) return st;
-  return launch_inverse<T, OP>(h, n, PtrArr<T>{A}, lda, batch, info,
-                               OP == INV_TRTRI && is_unit(diag));
+  return launch_inverse_uplo<T, OP>(h, is_upper(uplo), n, PtrArr<T>{A}, lda, batch, info,
+                                    OP == INV_TRTRI && is_unit(diag));
 }
 
 }  // namespace kgb

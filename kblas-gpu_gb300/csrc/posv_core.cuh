@@ -20,7 +20,8 @@
 //      certifies a normwise backward error below 10 n eps64 -- else
 //      x += S Ls^-T Ls^-1 S r (FP32 solve, FP64 update);
 //   4. a system whose FP32 factorization fails, or whose refinement stalls
-//      (error not halved) or runs out of steps, is factored again in FP64 by
+//      (error not halved), converges too slowly to beat an FP64 re-solve
+//      (refine_too_slow) or runs out of steps, is factored again in FP64 by
 //      the same team and solved directly; A then receives the FP64 factor and
 //      info the exact LAPACK code; iter[] records which path was taken.
 //  PLAIN (FP64 POSV): FP64 factor, solve, write L and X (LAPACK DPOSV).
@@ -54,6 +55,19 @@ constexpr double PC_EPS64 = 1.1102230246251565e-16;  // 2^-53, FP64 unit roundof
 // which the 0.99 u of slack covers.
 __host__ __device__ __forceinline__ double posv_eta_target(int n) {
   return (9.0 * n - 2.0) * PC_EPS64;
+}
+
+// Cost-model exit from refinement. A residual sweep over nr right-hand sides
+// costs n^2 nr FP64 FMAs; re-solving in FP64 costs n^3/6 (factor) + n^2 nr
+// (solve), i.e. n / (6 nr) + 1 sweeps. When the observed contraction
+// eta / eta_prev predicts more sweeps than that before eta reaches the
+// target, the FP64 path is the cheaper way to the same guarantee.
+__device__ __forceinline__ bool refine_too_slow(double eta, double eta_prev, double tol, int n,
+                                                int nr) {
+  if (!(eta_prev < INFINITY) || !(eta > tol)) return false;
+  const float rho = (float)(eta / eta_prev);   // in (0, 0.5] here
+  const float need = log2f((float)(eta / tol)) / -log2f(rho);
+  return need > (float)n / (6.0f * (float)nr) + 1.0f;
 }
 
 struct PosvCfg {
@@ -200,8 +214,11 @@ __device__ int small_fp64_posv(bool active, int n, int m, int r_from, double *A,
   }
   const bool solve = active && !fail;
   const int m_hi = warp_uniform_max_w(active ? m : 0, W);
-  for (int r0 = r_from; r0 < m_hi; r0++) {
-    const bool go = solve && r0 < m;
+  // Every lane of the warp runs the same trip count (small_llt_solve shuffles
+  // over the full warp); r_from differs between the systems sharing a warp,
+  // so each one solves only its own rows r_from..m-1.
+  for (int r0 = 0; r0 < m_hi; r0++) {
+    const bool go = solve && r0 >= r_from && r0 < m;
     double y = (go && lane < n) ? B[(size_t)r0 + (size_t)lane * ldb] : 0.0;
     y = small_llt_solve<double, W>(n, Ls64, rinv64, y);
     if (go && lane < n) B[(size_t)r0 + (size_t)lane * ldb] = y;
@@ -265,7 +282,8 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
         if (eta <= tol_conv) {
           going = false;
           converged = true;
-        } else if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) {
+        } else if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX ||
+                   refine_too_slow(eta, eta_prev, tol_conv, n, 1)) {
           going = false;
         } else {
           eta_prev = eta;
@@ -508,7 +526,9 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
         converged = true;
         break;
       }
-      if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX) break;
+      if (!(eta <= 0.5 * eta_prev) || step >= PC_ITMAX ||
+          refine_too_slow(eta, eta_prev, tol_conv, n, nr))
+        break;
       eta_prev = eta;
       for (int q = 0; q < nr; q++)
         for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = f64_to_f32_scaled(r[q * n + i], sh[i]);

@@ -16,6 +16,8 @@
 #include "kblas_internal.h"
 #include "launch_util.h"
 #include "posv_launch.h"
+#include "tri_internal.h"
+#include "uplo_swap.cuh"
 
 namespace kgb {
 
@@ -111,28 +113,105 @@ static int try_persistent(KBlasHandle *h, int op, int m, int n, AccA A, int lda,
 static inline int check_potrf(KBlasHandle *h, char uplo, int n, const void *A, int lda,
                               int batch) {
   if (!h) return KBLAS_Error_NotInitialized;
-  if (is_upper(uplo)) {
-    printf("Upper POTRF_BATCH is not implemented yet\n");
-    return KBLAS_NotImplemented;
-  }
-  if (!is_lower(uplo)) return KBLAS_Error_WrongInput;
+  if (!is_lower(uplo) && !is_upper(uplo)) return KBLAS_Error_WrongInput;
   if (n < 0 || batch < 0 || lda < (n > 1 ? n : 1)) return KBLAS_Error_WrongInput;
   if (n > 0 && batch > 0 && !A) return KBLAS_Error_WrongInput;
   return KBLAS_Success;
 }
 
+// B is m x n in both sides; A is n x n for side 'R' (X A = B) and m x m for
+// side 'L' (A X = B), the TRSM convention of the reference header.
 static inline int check_potrs(KBlasHandle *h, char side, char uplo, int m, int n, const void *A,
-                              int lda, const void *B, int ldb, int batch, const char *name) {
+                              int lda, const void *B, int ldb, int batch) {
   if (!h) return KBLAS_Error_NotInitialized;
-  if (is_left(side) || is_upper(uplo)) {
-    printf("(Left | Upper) %s_BATCH is not implemented yet\n", name);
-    return KBLAS_NotImplemented;
-  }
-  if (!is_right(side) || !is_lower(uplo)) return KBLAS_Error_WrongInput;
-  if (m < 0 || n < 0 || batch < 0 || lda < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1))
+  if (!(is_left(side) || is_right(side)) || !(is_lower(uplo) || is_upper(uplo)))
     return KBLAS_Error_WrongInput;
-  if (n > 0 && batch > 0 && (!A || (m > 0 && !B))) return KBLAS_Error_WrongInput;
+  const int order = is_left(side) ? m : n;
+  if (m < 0 || n < 0 || batch < 0 || lda < (order > 1 ? order : 1) || ldb < (m > 1 ? m : 1))
+    return KBLAS_Error_WrongInput;
+  if (order > 0 && batch > 0 && (!A || (m > 0 && n > 0 && !B))) return KBLAS_Error_WrongInput;
   return KBLAS_Success;
+}
+
+// ------------------------------ drivers ---------------------------------
+// Lower factorization of order n on the fastest path available.
+template <typename T, class AccA>
+static int potrf_lower(KBlasHandle *h, int n, AccA A, int lda, long long batch, int *info) {
+  int st = try_persistent<T>(h, 1, 0, n, A, lda, AccA{}, 1, (int)batch, info);
+  if (st != KBLAS_InsufficientWorkspace) return st;
+  return launch_chol<T, MODE_POTRF>(h, n, 0, A, lda, AccA{}, 1, batch, info);
+}
+
+// uplo = 'U': the lower kernels run between two in-place transposes
+// (uplo_swap.cuh); a kernel that did not launch leaves A as it was.
+template <typename T, class AccA>
+static int potrf_any(KBlasHandle *h, bool upper, int n, AccA A, int lda, long long batch,
+                     int *info) {
+  if (!upper) return potrf_lower<T>(h, n, A, lda, batch, info);
+  int st = swap_uplo<T>(h, n, A, lda, batch);
+  if (st != KBLAS_Success) return st;
+  st = potrf_lower<T>(h, n, A, lda, batch, info);
+  const int st2 = swap_uplo<T>(h, n, A, lda, batch);
+  return st != KBLAS_Success ? st : st2;
+}
+
+// Solve with a Cholesky factor by two TRSM passes (every side / uplo but
+// side 'R' + lower, which the fused kernels cover):
+//   side R, L: X L L^T = B     -> B L^-T, then L^-1 (reference Xpotrs_batch_drivers.cuh:94-171)
+//   side R, U: X U^T U = B     -> B U^-1, then U^-T
+//   side L, L: L L^T X = B     -> L^-1 B, then L^-T
+//   side L, U: U^T U X = B     -> U^-T B, then U^-1
+// skip (device info or null): systems whose factorization failed are left as is.
+template <typename T, class AccA, class AccB>
+static int potrs_trsm(KBlasHandle *h, char side, char uplo, int m, int n, AccA A, int lda, AccB B,
+                      int ldb, long long batch, const int *skip) {
+  const bool left = is_left(side), lower = is_lower(uplo);
+  const char first = (left == lower) ? 'N' : 'T';
+  const char second = (first == 'N') ? 'T' : 'N';
+  int st = trsm_batch_internal<T>(h, side, uplo, first, 'N', m, n, T(1), A, lda, B, ldb, batch, skip);
+  if (st != KBLAS_Success) return st;
+  return trsm_batch_internal<T>(h, side, uplo, second, 'N', m, n, T(1), A, lda, B, ldb, batch, skip);
+}
+
+template <typename T, class AccA, class AccB>
+static int potrs_any(KBlasHandle *h, char side, char uplo, int m, int n, AccA A, int lda, AccB B,
+                     int ldb, long long batch) {
+  if (batch == 0 || n == 0 || m == 0) return KBLAS_Success;
+  if (is_right(side) && is_lower(uplo)) {
+    int st = try_persistent<T>(h, 2, m, n, A, lda, B, ldb, (int)batch, nullptr);
+    if (st != KBLAS_InsufficientWorkspace) return st;
+    return launch_chol<T, MODE_POTRS>(h, n, m, A, lda, B, ldb, batch, nullptr);
+  }
+  return potrs_trsm<T>(h, side, uplo, m, n, A, lda, B, ldb, batch, nullptr);
+}
+
+template <typename T, class AccA, class AccB>
+static int posv_any(KBlasHandle *h, char side, char uplo, int m, int n, AccA A, int lda, AccB B,
+                    int ldb, long long batch, int *info) {
+  if (batch == 0) return KBLAS_Success;
+  const bool left = is_left(side), upper = is_upper(uplo);
+  const int order = left ? m : n, nrhs = left ? n : m;
+  if (order == 0) return zero_info(h, info, batch);
+  if (nrhs == 0) return potrf_any<T>(h, upper, order, A, lda, batch, info);
+  if (!left) {
+    // side R: the fused factor + solve kernels (on A^T for uplo 'U')
+    if (upper) {
+      int st = swap_uplo<T>(h, order, A, lda, batch);
+      if (st != KBLAS_Success) return st;
+    }
+    int st = try_persistent<T>(h, 0, m, n, A, lda, B, ldb, (int)batch, info);
+    if (st == KBLAS_InsufficientWorkspace)
+      st = launch_chol<T, MODE_POSV>(h, n, m, A, lda, B, ldb, batch, info);
+    if (upper) {
+      const int st2 = swap_uplo<T>(h, order, A, lda, batch);
+      if (st == KBLAS_Success) st = st2;
+    }
+    return st;
+  }
+  // side L: factor, then two TRSM passes that skip the systems whose info > 0
+  int st = potrf_any<T>(h, upper, order, A, lda, batch, info);
+  if (st != KBLAS_Success) return st;
+  return potrs_trsm<T>(h, side, uplo, m, n, A, lda, B, ldb, batch, info);
 }
 
 template <typename T>
@@ -143,10 +222,7 @@ static int potrf_strided(KBlasHandle *h, char uplo, int n, T *A, int lda, long l
   if (batch > 1 && sA < (long long)lda * n) return KBLAS_Error_WrongInput;
   if (batch == 0) return KBLAS_Success;
   if (n == 0) return zero_info(h, info, batch);
-  st = try_persistent<T>(h, 1, 0, n, Strided<T>{A, sA}, lda, Strided<T>{nullptr, 0}, 1, batch, info);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  return launch_chol<T, MODE_POTRF>(h, n, 0, Strided<T>{A, sA}, lda, Strided<T>{nullptr, 0}, 1,
-                                    batch, info);
+  return potrf_any<T>(h, is_upper(uplo), n, Strided<T>{A, sA}, lda, batch, info);
 }
 
 template <typename T>
@@ -155,70 +231,50 @@ static int potrf_array(KBlasHandle *h, char uplo, int n, T **A, int lda, int bat
   if (st != KBLAS_Success) return st;
   if (batch == 0) return KBLAS_Success;
   if (n == 0) return zero_info(h, info, batch);
-  st = try_persistent<T>(h, 1, 0, n, PtrArr<T>{A}, lda, PtrArr<T>{nullptr}, 1, batch, info);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  return launch_chol<T, MODE_POTRF>(h, n, 0, PtrArr<T>{A}, lda, PtrArr<T>{nullptr}, 1, batch, info);
+  return potrf_any<T>(h, is_upper(uplo), n, PtrArr<T>{A}, lda, batch, info);
 }
 
 template <typename T>
 static int potrs_strided(KBlasHandle *h, char side, char uplo, int m, int n, const T *A, int lda,
                          long long sA, T *B, int ldb, long long sB, int batch) {
-  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POTRS");
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch);
   if (st != KBLAS_Success) return st;
-  if (batch > 1 && sB < (long long)ldb * n) return KBLAS_Error_WrongInput;
-  if (batch == 0 || n == 0 || m == 0) return KBLAS_Success;
-  st = try_persistent<T>(h, 2, m, n, Strided<T>{const_cast<T *>(A), sA}, lda, Strided<T>{B, sB},
-                         ldb, batch, nullptr);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  return launch_chol<T, MODE_POTRS>(h, n, m, Strided<T>{const_cast<T *>(A), sA}, lda,
-                                    Strided<T>{B, sB}, ldb, batch, nullptr);
+  const int order = is_left(side) ? m : n;
+  if (batch > 1 && (sB < (long long)ldb * n || sA < (long long)lda * order))
+    return KBLAS_Error_WrongInput;
+  return potrs_any<T>(h, side, uplo, m, n, Strided<T>{const_cast<T *>(A), sA}, lda,
+                      Strided<T>{B, sB}, ldb, batch);
 }
 
 template <typename T>
 static int potrs_array(KBlasHandle *h, char side, char uplo, int m, int n, const T **A, int lda,
                        T **B, int ldb, int batch) {
-  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POTRS");
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch);
   if (st != KBLAS_Success) return st;
-  if (batch == 0 || n == 0 || m == 0) return KBLAS_Success;
-  st = try_persistent<T>(h, 2, m, n, PtrArr<T>{const_cast<T **>(A)}, lda, PtrArr<T>{B}, ldb, batch,
-                         nullptr);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  return launch_chol<T, MODE_POTRS>(h, n, m, PtrArr<T>{const_cast<T **>(A)}, lda, PtrArr<T>{B},
-                                    ldb, batch, nullptr);
+  return potrs_any<T>(h, side, uplo, m, n, PtrArr<T>{const_cast<T **>(A)}, lda, PtrArr<T>{B}, ldb,
+                      batch);
 }
 
 template <typename T>
 static int posv_strided(KBlasHandle *h, char side, char uplo, int m, int n, T *A, int lda,
                         long long sA, T *B, int ldb, long long sB, int batch, int *info) {
-  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POSV");
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch);
   if (st != KBLAS_Success) return st;
-  if (batch > 1 && (sA < (long long)lda * n || (m > 0 && sB < (long long)ldb * n)))
+  const int order = is_left(side) ? m : n;
+  if (batch > 1 && (sA < (long long)lda * order || (m > 0 && n > 0 && sB < (long long)ldb * n)))
     return KBLAS_Error_WrongInput;
-  if (batch == 0) return KBLAS_Success;
-  if (n == 0) return zero_info(h, info, batch);
-  st = try_persistent<T>(h, m == 0 ? 1 : 0, m, n, Strided<T>{A, sA}, lda, Strided<T>{B, sB}, ldb,
-                         batch, info);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  if (m == 0)
-    return launch_chol<T, MODE_POTRF>(h, n, 0, Strided<T>{A, sA}, lda, Strided<T>{nullptr, 0}, 1,
-                                      batch, info);
-  return launch_chol<T, MODE_POSV>(h, n, m, Strided<T>{A, sA}, lda, Strided<T>{B, sB}, ldb, batch,
-                                   info);
+  return posv_any<T>(h, side, uplo, m, n, Strided<T>{A, sA}, lda, Strided<T>{B, sB}, ldb, batch,
+                     info);
 }
 
 template <typename T>
 static int posv_array(KBlasHandle *h, char side, char uplo, int m, int n, T **A, int lda, T **B,
                       int ldb, int batch, int *info) {
-  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch, "POSV");
+  int st = check_potrs(h, side, uplo, m, n, A, lda, B, ldb, batch);
   if (st != KBLAS_Success) return st;
-  if (batch == 0) return KBLAS_Success;
-  if (n == 0) return zero_info(h, info, batch);
-  st = try_persistent<T>(h, m == 0 ? 1 : 0, m, n, PtrArr<T>{A}, lda, PtrArr<T>{m ? B : nullptr},
-                         ldb, batch, info);
-  if (st != KBLAS_InsufficientWorkspace) return st;
-  if (m == 0)
-    return launch_chol<T, MODE_POTRF>(h, n, 0, PtrArr<T>{A}, lda, PtrArr<T>{nullptr}, 1, batch, info);
-  return launch_chol<T, MODE_POSV>(h, n, m, PtrArr<T>{A}, lda, PtrArr<T>{B}, ldb, batch, info);
+  const int nrhs = is_left(side) ? n : m;
+  return posv_any<T>(h, side, uplo, m, n, PtrArr<T>{A}, lda, PtrArr<T>{nrhs ? B : nullptr}, ldb,
+                     batch, info);
 }
 
 }  // namespace kgb

@@ -226,6 +226,19 @@ void kblas_trsm_batch_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trsm_batch_strided_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trmm_batch_wsquery(kblasHandle_t, char, int, int, int) {}
 void kblas_trmm_batch_strided_wsquery(kblasHandle_t, char, int, int, int) {}
+// GEMM and the variable-size GEMM / SYRK need none either (reference
+// workspace_queries.cu:203-253 asks for cuBLAS pointer arrays and MAGMA's
+// size maxima). The variable-size TRSM recomputes max_m / max_n on the device
+// when the caller passes neither (reference workspace_queries.cu:268-278).
+void kblas_gemm_batch_strided_wsquery(kblasHandle_t, int) {}
+void kblas_gemm_batch_nonuniform_wsquery(kblasHandle_t) {}
+void kblas_syrk_batch_nonuniform_wsquery(kblasHandle_t) {}
+void kblas_trsm_batch_nonuniform_wsquery(kblasHandle_t h) {
+  if (!h) return;
+  KBlasWorkspaceState need;
+  need.d_data_bytes = 2 * sizeof(int);
+  h->ws.requested.pad(need);
+}
 // POTRF / POTRS / POSV: the double-precision routines of order 33..1024 run
 // on the persistent panel path when this workspace is allocated (else on the
 // one-launch blocked kernel, which needs none).

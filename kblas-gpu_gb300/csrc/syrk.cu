@@ -1,8 +1,9 @@
-// syrk.cu -- batched SYRK (lower), single and double precision, strided and
+// syrk.cu -- batched SYRK (lower and upper), single and double precision, strided and
 // pointer-array forms: C := alpha * op(A) * op(A)^T + beta * C.
 //
 // Entry points replace reference src/batch_triangular/Xsyrk_batch.cu:83-200
-// (Upper -> KBLAS_NotImplemented as Xsyrk_batch_drivers.cuh:133-136). The
+// (Upper is KBLAS_NotImplemented there, Xsyrk_batch_drivers.cuh:133-136; here
+// it runs on the C-tile engine of gemm_tile.cuh). The
 // reference builds pointer arrays and issues one cuBLAS gemmBatched per level
 // of a flat recursion plus a diagonal-tile kernel; here one launch covers all
 // lower tiles of every matrix: one CTA per (matrix, 32 x 32 lower tile), the
@@ -11,6 +12,7 @@
 #include <stdio.h>
 
 #include "device_util.cuh"
+#include "gemm_tile.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
 
@@ -79,6 +81,20 @@ syrk_lower_kernel(int m, int k, int trans, T alpha, AccA A, int lda, T beta, Acc
     }
 }
 
+// uplo 'U' (KBLAS_NotImplemented in the reference): the C-tile engine of
+// gemm_tile.cuh on the upper tile triangle.
+template <typename T, class AccA, class AccC>
+static int launch_syrk_upper(KBlasHandle *h, int m, int k, bool trans, T alpha, AccA A, int lda,
+                             T beta, AccC Cm, int ldc, long long batch) {
+  if (batch > 0x7fffffffLL) return KBLAS_NotSupported;
+  const long long nt = (m + GT - 1) / GT;
+  dim3 grid((unsigned)batch, tile_slots(h, batch, nt * (nt + 1) / 2));
+  syrk_batch_kernel<T><<<grid, GT_NT, 0, h->stream>>>(1, trans ? 1 : 0, alpha, A, beta, Cm,
+                                                      DimsU<4>{{m, k, lda, ldc}}, batch);
+  KGB_LAUNCH_CHECK("syrk_batch_kernel");
+  return KBLAS_Success;
+}
+
 template <typename T, class AccA, class AccC>
 static int launch_syrk(KBlasHandle *h, int m, int k, bool trans, T alpha, AccA A, int lda, T beta,
                        AccC Cm, int ldc, long long batch) {
@@ -94,11 +110,8 @@ static int launch_syrk(KBlasHandle *h, int m, int k, bool trans, T alpha, AccA A
 static inline int check_syrk(KBlasHandle *h, char uplo, char trans, int m, int n, int lda, int ldb,
                              int batch) {
   if (!h) return KBLAS_Error_NotInitialized;
-  if (is_upper(uplo)) {
-    printf("Upper SYRK_BATCH is not implemented yet\n");
-    return KBLAS_NotImplemented;
-  }
-  if (!is_lower(uplo) || !(is_trans(trans) || is_notrans(trans))) return KBLAS_Error_WrongInput;
+  if (!(is_lower(uplo) || is_upper(uplo)) || !(is_trans(trans) || is_notrans(trans)))
+    return KBLAS_Error_WrongInput;
   const int rows_a = is_notrans(trans) ? m : n;
   if (m < 0 || n < 0 || batch < 0 || lda < (rows_a > 1 ? rows_a : 1) || ldb < (m > 1 ? m : 1))
     return KBLAS_Error_WrongInput;
@@ -112,6 +125,9 @@ static int syrk_strided(KBlasHandle *h, char uplo, char trans, int m, int n, T a
   if (st != KBLAS_Success) return st;
   if (m == 0 || batch == 0) return KBLAS_Success;
   if (!B || (n > 0 && !A) || (batch > 1 && sB < (long long)ldb * m)) return KBLAS_Error_WrongInput;
+  if (is_upper(uplo))
+    return launch_syrk_upper<T>(h, m, n, is_trans(trans), alpha, Strided<T>{const_cast<T *>(A), sA},
+                                lda, beta, Strided<T>{B, sB}, ldb, batch);
   return launch_syrk<T>(h, m, n, is_trans(trans), alpha, Strided<T>{const_cast<T *>(A), sA}, lda,
                         beta, Strided<T>{B, sB}, ldb, batch);
 }
@@ -123,6 +139,9 @@ static int syrk_array(KBlasHandle *h, char uplo, char trans, int m, int n, T alp
   if (st != KBLAS_Success) return st;
   if (m == 0 || batch == 0) return KBLAS_Success;
   if (!B || (n > 0 && !A)) return KBLAS_Error_WrongInput;
+  if (is_upper(uplo))
+    return launch_syrk_upper<T>(h, m, n, is_trans(trans), alpha, PtrArr<T>{const_cast<T **>(A)}, lda,
+                                beta, PtrArr<T>{B}, ldb, batch);
   return launch_syrk<T>(h, m, n, is_trans(trans), alpha, PtrArr<T>{const_cast<T **>(A)}, lda, beta,
                         PtrArr<T>{B}, ldb, batch);
 }

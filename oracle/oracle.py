@@ -62,6 +62,9 @@ def lib():
                 getattr(L, f"oracle_{pfx}trsm_batch").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, Lg, P, I, Lg, I, I]
                 getattr(L, f"oracle_{pfx}trmm_batch").argtypes = [Ch, Ch, Ch, Ch, I, I, R, P, I, Lg, P, I, Lg, I, I]
                 getattr(L, f"oracle_{pfx}syrk_batch").argtypes = [Ch, Ch, I, I, R, P, I, Lg, R, P, I, Lg, I, I]
+                getattr(L, f"oracle_{pfx}gemm").argtypes = [Ch, Ch, I, I, I, R, P, I, P, I, R, P, I]
+                getattr(L, f"oracle_{pfx}gemm_batch").argtypes = [Ch, Ch, I, I, I, R, P, I, Lg, P, I, Lg,
+                                                                  R, P, I, Lg, I, I]
                 getattr(L, f"oracle_{pfx}posv_vbatch").argtypes = [P, P, P, P, P, P, I, P, I]
                 getattr(L, f"oracle_{pfx}trtri_batch").argtypes = [I, I, P, I, Lg, I, P, I]
                 getattr(L, f"oracle_{pfx}lauum_batch").argtypes = [I, P, I, Lg, I, I]
@@ -155,6 +158,64 @@ def syrk_batch(uplo, trans, m, k, alpha, A, beta, Cm, nthreads=None):
     getattr(lib(), f"oracle_{_pfx(A)}syrk_batch")(_b(uplo), _b(trans), m, k, alpha, _p(A), lda,
                                                   ncol * lda, beta, _p(Cm), ldc, ncolc * ldc,
                                                   batch, nthreads or nthreads_default())
+
+
+def gemm_batch(transA, transB, m, n, k, alpha, A, B, beta, Cm, nthreads=None):
+    """C := alpha op(A) op(B) + beta C over a (batch, ncol, ld) column-major stack."""
+    batch, ncol, lda = A.shape
+    _, ncolb, ldb = B.shape
+    _, ncolc, ldc = Cm.shape
+    getattr(lib(), f"oracle_{_pfx(A)}gemm_batch")(_b(transA), _b(transB), m, n, k, alpha, _p(A),
+                                                  lda, ncol * lda, _p(B), ldb, ncolb * ldb, beta,
+                                                  _p(Cm), ldc, ncolc * ldc, batch,
+                                                  nthreads or nthreads_default())
+
+
+def _swap_uplo(A: np.ndarray, n: int):
+    """Transpose the leading n x n block of every matrix in place."""
+    A[:, :n, :n] = A[:, :n, :n].transpose(0, 2, 1).copy()
+
+
+def potrf_batch_uplo(A: np.ndarray, n: int, uplo: str, nthreads=None):
+    """xPOTRF for either triangle (only that triangle referenced, LAPACK): the
+    upper factor U of A = U^T U is the transpose of the lower factor of A^T,
+    so uplo 'U' runs the lower restatement between two transposes."""
+    if uplo == "L":
+        return potrf_batch(A, n, nthreads)
+    _swap_uplo(A, n)
+    info = potrf_batch(A, n, nthreads)
+    _swap_uplo(A, n)
+    return info
+
+
+_POTRS_SEQ = {("R", "L"): ("T", "N"), ("R", "U"): ("N", "T"),
+              ("L", "L"): ("N", "T"), ("L", "U"): ("T", "N")}
+
+
+def potrs_batch_side(side: str, uplo: str, m: int, n: int, F: np.ndarray, B: np.ndarray,
+                     nthreads=None):
+    """xPOTRS with the factor F of either triangle, for A X = B (side 'L', A
+    m x m, LAPACK xPOTRS: two triangular solves, dpotrs.f) or X A = B (side
+    'R', A n x n); B is m x n. The two TRSM passes:
+      R,L: B L^-T then L^-1   R,U: B U^-1 then U^-T
+      L,L: L^-1 B then L^-T   L,U: U^-T B then U^-1"""
+    t1, t2 = _POTRS_SEQ[(side, uplo)]
+    trsm_batch(side, uplo, t1, "N", m, n, 1.0, F, B, nthreads)
+    trsm_batch(side, uplo, t2, "N", m, n, 1.0, F, B, nthreads)
+
+
+def posv_batch_side(side: str, uplo: str, m: int, n: int, A: np.ndarray, B: np.ndarray,
+                    nthreads=None):
+    """xPOSV for every side / uplo: factor, then solve the systems whose info
+    is 0 (the others keep B, LAPACK)."""
+    order = m if side == "L" else n
+    info = potrf_batch_uplo(A, order, uplo, nthreads)
+    ok = np.where(info == 0)[0]
+    if len(ok):
+        Fa, Bb = np.ascontiguousarray(A[ok]), np.ascontiguousarray(B[ok])
+        potrs_batch_side(side, uplo, m, n, Fa, Bb, nthreads)
+        B[ok] = Bb
+    return info
 
 
 def backward_error_r(A: np.ndarray, X: np.ndarray, B: np.ndarray, m: int, n: int,

@@ -162,6 +162,30 @@ void ORC(syrk)(char uplo, char trans, int m, int k, REAL alpha, const REAL *A, i
     }
 }
 
+/* BLAS xGEMM: C := alpha*op(A)*op(B) + beta*C, C m x n, op(A) m x k,
+ * op(B) k x n; op(A), op(B) not read when alpha == 0 or k == 0, C not read
+ * when beta == 0 (the reference BLAS rules, which the reference's cuBLAS
+ * and MAGMA calls, src/batch_triangular/Xgemm_batch_core.cuh:171-470, keep). */
+void ORC(gemm)(char transA, char transB, int m, int n, int k, REAL alpha, const REAL *A,
+               int lda, const REAL *B, int ldb, REAL beta, REAL *C, int ldc)
+{
+    int ta = (transA == 'T' || transA == 't' || transA == 'C' || transA == 'c');
+    int tb = (transB == 'T' || transB == 't' || transB == 'C' || transB == 'c');
+    int prod = (alpha != (REAL)0 && k > 0);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            REAL s = 0;
+            if (prod)
+                for (int l = 0; l < k; l++) {
+                    REAL a = ta ? AT(A, lda, l, i) : AT(A, lda, i, l);
+                    REAL b = tb ? AT(B, ldb, j, l) : AT(B, ldb, l, j);
+                    s += a * b;
+                }
+            REAL c = (beta == (REAL)0) ? (REAL)0 : beta * AT(C, ldc, i, j);
+            AT(C, ldc, i, j) = prod ? alpha * s + c : c;
+        }
+}
+
 /* POTRS with side 'R', uplo 'L' (the only form of the reference,
  * src/batch_triangular/Xpotrs_batch_drivers.cuh:40-43): X*L*L^T = B, i.e.
  * B := B*L^{-T}*L^{-1}, the reference's TRSM(R,L,T,N) then TRSM(R,L,N,N)
@@ -305,6 +329,16 @@ void ORC(syrk_batch)(char uplo, char trans, int m, int k, REAL alpha, const REAL
     for (int b = 0; b < batch; b++)
         ORC(syrk)(uplo, trans, m, k, alpha, A + (size_t)b * strideA, lda, beta,
                   C + (size_t)b * strideC, ldc);
+}
+
+void ORC(gemm_batch)(char transA, char transB, int m, int n, int k, REAL alpha, const REAL *A,
+                     int lda, long strideA, const REAL *B, int ldb, long strideB, REAL beta,
+                     REAL *C, int ldc, long strideC, int batch, int nthreads)
+{
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++)
+        ORC(gemm)(transA, transB, m, n, k, alpha, A + (size_t)b * strideA, lda,
+                  B + (size_t)b * strideB, ldb, beta, C + (size_t)b * strideC, ldc);
 }
 
 void ORC(trtri_batch)(int unit, int n, REAL *A, int lda, long strideA, int batch, int *info,

@@ -5,7 +5,8 @@ looped over the batch (testing/batch_triangular/test_Xpotrf_batch.cpp:317-338,
 test_Xposv_batch.cpp:313-338, test_Xtrsm_batch.cpp:330-360,
 test_Xtrmm_batch.cpp:346-354, test_Xsyrk_batch.cpp:405-417) and ship no golden
 vectors of their own. This script records what LAPACK/BLAS (scipy's bundled
-OpenBLAS: dpotrf/spotrf, dpotrs, dtrsm/strsm, dtrmm/strmm, dsyrk/ssyrk)
+OpenBLAS: dpotrf/spotrf, dpotrs, dtrsm/strsm, dtrmm/strmm, dsyrk/ssyrk,
+dgemm/sgemm, and the xTRTRI / xLAUUM / xPOTRI inversion routines)
 returns on small seeded inputs, including non-SPD matrices with a known
 failing leading minor, so tests/test_oracle.py can check the C oracle against
 it on any machine (scipy is not needed at test time).
@@ -133,6 +134,59 @@ def main():
             assert info == k, (n, k, info)
             out[f"{name}trtri_sing_n{n}_L"] = c
             out[f"{name}trtri_sing_n{n}_info"] = np.int32(info)
+    # GEMM (every transA / transB, alpha, beta incl. 0) and upper SYRK, on a
+    # third stream so the arrays above do not change
+    r3 = rng(2026, 2)
+    for dt, name in ((np.float64, "d"), (np.float32, "s")):
+        gemm, syrk = (blas.dgemm, blas.dsyrk) if name == "d" else (blas.sgemm, blas.ssyrk)
+        for (m, n, k) in ((1, 1, 1), (5, 7, 3), (16, 16, 16), (33, 17, 40), (64, 9, 70), (3, 50, 0)):
+            for ta in "NT":
+                for tb in "NT":
+                    a = r3.standard_normal((m, k) if ta == "N" else (k, m))
+                    b = r3.standard_normal((k, n) if tb == "N" else (n, k))
+                    c0 = r3.standard_normal((m, n))
+                    alpha, beta = (1.5, -0.5) if (m + n) % 2 else (-1.0, 0.0)
+                    res = gemm(alpha, a.astype(dt), b.astype(dt), beta=beta, c=c0.astype(dt),
+                               trans_a=int(ta == "T"), trans_b=int(tb == "T"))
+                    key = f"{name}gemm_{ta}{tb}_m{m}_n{n}_k{k}"
+                    out[key + "_A"] = a.astype(dt)
+                    out[key + "_B"] = b.astype(dt)
+                    out[key + "_C"] = c0.astype(dt)
+                    out[key + "_ab"] = np.array([alpha, beta])
+                    out[key + "_R"] = res
+        for (m, k) in ((5, 3), (33, 17), (48, 40)):
+            for trans in "NT":
+                a = r3.standard_normal((m, k) if trans == "N" else (k, m))
+                c0 = spd(m, r3)
+                res = syrk(-1.0, a.astype(dt), beta=1.0, c=c0.astype(dt),
+                           trans=int(trans == "T"), lower=0)
+                key = f"{name}syrku_{trans}_m{m}_k{k}"
+                out[key + "_A"] = a.astype(dt)
+                out[key + "_C"] = c0.astype(dt)
+                out[key + "_R"] = np.triu(res)
+    # Upper-triangle xPOTRF and side-L xPOTRS for both triangles (LAPACK's own
+    # side), on a fourth stream
+    r4 = rng(2027, 3)
+    for dt, name in ((np.float64, "d"), (np.float32, "s")):
+        potrf, potrs = (lapack.dpotrf, lapack.dpotrs) if name == "d" else (lapack.spotrf, lapack.spotrs)
+        for n in (1, 3, 16, 33, 64, 97):
+            a = spd(n, r4).astype(dt)
+            b = r4.standard_normal((n, 3)).astype(dt)
+            for uplo in "LU":
+                c, info = potrf(a, lower=int(uplo == "L"), clean=1)
+                assert info == 0
+                x, info = potrs(c, b, lower=int(uplo == "L"))
+                assert info == 0
+                key = f"{name}potrf{uplo.lower()}_n{n}"
+                out[key + "_A"] = a
+                out[key + "_F"] = c
+                out[key + "_B"] = b
+                out[key + "_X"] = x
+        a = spd(40, r4)
+        a[17, 17] = -1.0
+        c, info = lapack.dpotrf(a, lower=0, clean=0)
+        out["dpotrfu_bad_n40_A"] = a
+        out["dpotrfu_bad_n40_info"] = np.int32(info)
     path = os.path.join(HERE, "lapack_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, len(out), "arrays", os.path.getsize(path), "bytes")

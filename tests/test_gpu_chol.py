@@ -213,12 +213,13 @@ def test_argument_errors(gpu, handle, kb):
     d = gpu.zeros(256, dtype=gpu.float64, device="cuda")
     info = gpu.zeros(4, dtype=gpu.int32, device="cuda")
     p, ip = d.data_ptr(), info.data_ptr()
-    NI, WI = kb.KBLAS_NotImplemented, kb.KBLAS_Error_WrongInput
-    # reference behaviour: Upper / Left are not implemented
-    assert handle.call("kblasDpotrf_batch_strided", "U", 8, p, 8, 64, 1, ip) == NI
-    assert handle.call("kblasDposv_batch_strided", "L", "L", 1, 8, p, 8, 64, p, 1, 8, 1, ip) == NI
-    assert handle.call("kblasDpotrs_batch_strided", "R", "U", 1, 8, p, 8, 64, p, 1, 8, 1) == NI
-    assert handle.call("kblasDsyrk_batch_strided", "U", "N", 8, 8, 1.0, p, 8, 64, 0.0, p, 8, 64, 1) == NI
+    WI = kb.KBLAS_Error_WrongInput
+    # Upper / Left POTRF, POTRS, POSV and Upper SYRK are implemented here (the
+    # reference returns KBLAS_NotImplemented); malformed flags are still errors
+    assert handle.call("kblasDpotrs_batch_strided", "X", "U", 1, 8, p, 8, 64, p, 1, 8, 1) == WI
+    assert handle.call("kblasDposv_batch_strided", "L", "Q", 1, 8, p, 8, 64, p, 1, 8, 1, ip) == WI
+    # side L: A is m x m, so lda < m is an error
+    assert handle.call("kblasDposv_batch_strided", "L", "L", 8, 1, p, 7, 64, p, 8, 8, 1, ip) == WI
     # malformed arguments
     assert handle.call("kblasDpotrf_batch_strided", "L", -1, p, 8, 64, 1, ip) == WI
     assert handle.call("kblasDpotrf_batch_strided", "L", 8, p, 7, 64, 1, ip) == WI

@@ -1,6 +1,7 @@
-"""GPU parity of the batched inversion routines (lower): TRTRI, LAUUM, POTRI,
-POTI, S and D, strided and pointer-array forms, against the CPU oracle (itself
-pinned to LAPACK in test_oracle.py).
+"""GPU parity of the batched inversion routines (lower; the upper forms are in
+test_gpu_uplo_side.py): TRTRI, LAUUM, POTRI, POTI, S and D, strided and
+pointer-array forms, against the CPU oracle (itself pinned to LAPACK in
+test_oracle.py).
 
 Bars: FP64 results within 100 n eps of the oracle relative to the largest
 entry (the inverse amplifies rounding by the conditioning; the matrices here
@@ -118,13 +119,3 @@ def test_trtri_unit_diagonal(gpu, handle, wl, orc):
     out = dev.cpu().numpy()
     assert np.array_equal(np.diagonal(out, axis1=1, axis2=2), np.diagonal(L, axis1=1, axis2=2))
     assert rel_lower(out, ref, n) <= 100 * n * eps(np.float64)
-
-
-@pytest.mark.parametrize("op", ["trtri", "lauum", "potri", "poti"])
-def test_upper_not_implemented(gpu, handle, op):
-    info = gpu.zeros(1, dtype=gpu.int32, device="cuda")
-    a = gpu.zeros(16, dtype=gpu.float64, device="cuda")
-    args_d = ("N",) if op == "trtri" else ()
-    st = handle.call(f"kblasD{op}_batch_strided", "U", *args_d, 4, a.data_ptr(), 4, 16, 1,
-                     info.data_ptr())
-    assert st == -2

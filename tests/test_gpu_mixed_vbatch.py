@@ -86,6 +86,22 @@ def test_mixed_illconditioned_cond_1e2_to_1e8(gpu, handle, kb, wl, orc):
     assert (it[cond < 1e4] >= 0).all()
 
 
+@pytest.mark.parametrize("n", [8, 16, 24])
+def test_mixed_register_path_illconditioned_many_rhs(gpu, handle, kb, wl, orc, n):
+    """Register path (several systems share a warp) with cond up to 1e8 and 4
+    right-hand sides: systems fall back to FP64 after different numbers of
+    converged right-hand sides, so the systems of one warp resume the FP64
+    solve at different rows; every system must still meet the bar."""
+    m, batch = 4, 512
+    a, cond = wl.spd_cond(batch, n, seed=21 + n)
+    b = wl.rhs_rows(batch, m, n, seed=22 + n)
+    A, X, info, it = run_uniform_mixed(gpu, kb, handle, a, b, m, n)
+    assert (info == 0).all()
+    eta = orc.backward_error_r(a, X, b, m, n)
+    assert eta.max() <= 10 * n * EPS64, eta.max()
+    assert (it < 0).any() and (it >= 0).any()
+
+
 def test_mixed_indefinite_info_exact(gpu, handle, kb, wl, orc):
     n, m, batch = 48, 2, 40
     a = wl.spd_shifted(batch, n, seed=11)

@@ -101,39 +101,43 @@ def test_trsm_alpha_zero_does_not_read_A(gpu, handle, dt):
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["d", "s"])
+@pytest.mark.parametrize("uplo", ["L", "U"])
 @pytest.mark.parametrize("trans", ["N", "T"])
 @pytest.mark.parametrize("mk", [(1, 1), (5, 3), (16, 16), (33, 17), (64, 64), (70, 9), (100, 130)])
 @pytest.mark.parametrize("form", ["strided", "array"])
-def test_syrk(gpu, handle, wl, orc, dt, trans, mk, form):
+def test_syrk(gpu, handle, wl, orc, dt, uplo, trans, mk, form):
     m, k = mk
     batch = 11
     rows, cols = (m, k) if trans == "N" else (k, m)
     lda, ldc = rows + 1, m + 2
     a = wl.general(batch, rows, cols, seed=m + 3 * k, ld=lda).astype(dt)
     c = wl.spd_shifted(batch, m, seed=m, ld=ldc).astype(dt)
-    # sentinel above the diagonal of C must survive
+    # sentinel in the triangle of C that is not referenced must survive
+    # (column j of the column-major batch holds rows 0..ld-1)
+    other = [slice(0, j) if uplo == "L" else slice(j + 1, m) for j in range(m)]
     for j in range(m):
-        c[:, j, :j] = -3.5
+        c[:, j, other[j]] = -3.5
     ref = c.copy()
-    orc.syrk_batch("L", trans, m, k, -1.0, a, 1.0, ref)
+    orc.syrk_batch(uplo, trans, m, k, -1.0, a, 1.0, ref)
     pfx = "D" if dt == np.float64 else "S"
     da, dc = to_dev(gpu, a), to_dev(gpu, c)
     if form == "strided":
-        st = handle.call(f"kblas{pfx}syrk_batch_strided", "L", trans, m, k, -1.0, da.data_ptr(), lda,
+        st = handle.call(f"kblas{pfx}syrk_batch_strided", uplo, trans, m, k, -1.0, da.data_ptr(), lda,
                          cols * lda, 1.0, dc.data_ptr(), ldc, m * ldc, batch)
     else:
         pa, pc = ptr_array(gpu, da), ptr_array(gpu, dc)
-        st = handle.call(f"kblas{pfx}syrk_batch", "L", trans, m, k, -1.0, pa.data_ptr(), lda, 1.0,
+        st = handle.call(f"kblas{pfx}syrk_batch", uplo, trans, m, k, -1.0, pa.data_ptr(), lda, 1.0,
                          pc.data_ptr(), ldc, batch)
     assert st == 1
     gpu.cuda.synchronize()
     out = dc.cpu().numpy()
     for j in range(m):
-        assert (out[:, j, :j] == -3.5).all(), "upper triangle of C written"
+        assert (out[:, j, other[j]] == -3.5).all(), "unreferenced triangle of C written"
         assert np.array_equal(out[:, j, m:], c[:, j, m:]), "ldc padding written"
     A = dense(a.astype(np.float64), rows, cols)
     opA = A if trans == "N" else A.transpose(0, 2, 1)
     scale = np.abs(opA) @ np.abs(opA).transpose(0, 2, 1) + np.abs(dense(c.astype(np.float64), m, m))
-    G = np.tril(dense(out.astype(np.float64), m, m))
-    R = np.tril(dense(ref.astype(np.float64), m, m))
-    assert (np.abs(G - R) <= 10 * max(k, 1) * eps(dt) * np.tril(scale) + 1e-300).all()
+    tri = np.tril if uplo == "L" else np.triu
+    G = tri(dense(out.astype(np.float64), m, m))
+    R = tri(dense(ref.astype(np.float64), m, m))
+    assert (np.abs(G - R) <= 10 * max(k, 1) * eps(dt) * tri(scale) + 1e-300).all()

@@ -103,6 +103,74 @@ def test_syrk_vs_blas(golden, orc, pfx):
         assert np.abs(got - ref).max() <= 10 * k * eps(dt) * scale, c
 
 
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_gemm_vs_blas(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    cases = keys(golden, rf"{pfx}gemm_(\w\w_m\d+_n\d+_k\d+)_A")
+    assert len(cases) == 24
+    for c in cases:
+        tt, ms, ns, ks = c.split("_")
+        m, n, k = int(ms[1:]), int(ns[1:]), int(ks[1:])
+        g = {x: golden[f"{pfx}gemm_{c}_{x}"] for x in ("A", "B", "C", "ab", "R")}
+        a, b, cm = colmajor(g["A"], dt), colmajor(g["B"], dt), colmajor(g["C"], dt)
+        alpha, beta = (float(v) for v in g["ab"])
+        orc.gemm_batch(tt[0], tt[1], m, n, k, alpha, a, b, beta, cm, nthreads=1)
+        got = cm[0].T
+        scale = (abs(beta) * np.abs(g["C"]).max() + abs(alpha) * k * np.abs(g["A"]).max(initial=0)
+                 * np.abs(g["B"]).max(initial=0) + 1e-30)
+        assert np.abs(got - g["R"]).max() <= 10 * max(k, 1) * eps(dt) * scale, c
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_syrk_upper_vs_blas(golden, orc, pfx):
+    dt = np.float64 if pfx == "d" else np.float32
+    cases = keys(golden, rf"{pfx}syrku_(\w_m\d+_k\d+)_A")
+    assert cases
+    for c in cases:
+        trans, ms, ks = c.split("_")
+        m, k = int(ms[1:]), int(ks[1:])
+        a = colmajor(golden[f"{pfx}syrku_{c}_A"], dt)
+        cm = colmajor(golden[f"{pfx}syrku_{c}_C"], dt)
+        orc.syrk_batch("U", trans, m, k, -1.0, a, 1.0, cm, nthreads=1)
+        got = np.triu(cm[0].T)
+        scale = np.abs(golden[f"{pfx}syrku_{c}_C"]).max() + k * np.abs(golden[f"{pfx}syrku_{c}_A"]).max() ** 2
+        assert np.abs(got - golden[f"{pfx}syrku_{c}_R"]).max() <= 10 * k * eps(dt) * scale, c
+        # the strict lower triangle is not touched
+        c0 = golden[f"{pfx}syrku_{c}_C"].astype(dt)
+        assert np.array_equal(np.tril(cm[0].T, -1), np.tril(c0, -1))
+
+
+@pytest.mark.parametrize("pfx", ["d", "s"])
+def test_potrf_uplo_and_side_l_potrs_vs_lapack(golden, orc, pfx):
+    """Upper POTRF through the transposed lower restatement, and POTRS with
+    side 'L' (LAPACK's own xPOTRS) for both triangles, against LAPACK."""
+    dt = np.float64 if pfx == "d" else np.float32
+    ns = sorted(int(x) for x in keys(golden, rf"{pfx}potrfu_n(\d+)_A"))
+    assert ns
+    for n in ns:
+        for uplo in "LU":
+            g = {x: golden[f"{pfx}potrf{uplo.lower()}_n{n}_{x}"] for x in "AFBX"}
+            a = colmajor(g["A"], dt)
+            a_before = a.copy()
+            info = orc.potrf_batch_uplo(a, n, uplo, nthreads=1)
+            assert info[0] == 0
+            tri = np.triu if uplo == "U" else np.tril
+            F = tri(a[0].T)
+            assert np.abs(F - g["F"]).max() <= 10 * n * eps(dt) * np.abs(g["F"]).max(), (n, uplo)
+            other = np.tril(a[0].T, -1) if uplo == "U" else np.triu(a[0].T, 1)
+            other0 = np.tril(a_before[0].T, -1) if uplo == "U" else np.triu(a_before[0].T, 1)
+            assert np.array_equal(other, other0), "the other triangle was written"
+            b = colmajor(g["B"], dt)           # n x 3, column-major
+            orc.potrs_batch_side("L", uplo, n, 3, a, b, nthreads=1)
+            X = b[0].T
+            scale = np.abs(g["X"]).max()
+            assert np.abs(X - g["X"]).max() <= 1e3 * n * eps(dt) * scale, (n, uplo)
+    if pfx == "d":
+        a = colmajor(golden["dpotrfu_bad_n40_A"])
+        info = orc.potrf_batch_uplo(a, 40, "U", nthreads=1)
+        assert info[0] == int(golden["dpotrfu_bad_n40_info"]) == 18
+
+
 def test_backward_error_detects_wrong_solution(orc):
     """A planted mistake in the solution must blow the backward error up."""
     rng = np.random.default_rng(1)
