@@ -26,6 +26,7 @@
 #ifndef KBLAS_GB300_BATCH_H
 #define KBLAS_GB300_BATCH_H
 
+#include <cuComplex.h>
 #include <cuda_runtime_api.h>
 #include "kblas_defs.h"
 
@@ -273,6 +274,157 @@ int kblasDtrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, ch
                       int *n, int max_m, int max_n, const double alpha, const double **A,
                       int *lda, double **B, int *ldb, int batchCount);
 
+
+/* ---------------------------------------------------------------------------
+ * Complex precisions C (cuFloatComplex) and Z (cuDoubleComplex) of every
+ * routine above, reference include/kblas_batch.h (kblas{C,Z}* names, e.g.
+ * :339-354, :438-453 for GEMM). As in the reference, these are the
+ * complex-symmetric forms: POTRF factors A = L*L^T (no conjugation; a pivot
+ * fails when it is zero or not finite, and its square root is the principal
+ * one), op = transpose for TRSM / TRMM / GEMM, SYRK forms A*A^T; the
+ * reference's tests build complex-symmetric matrices
+ * (testing/testing_helper.cu:405-414). Arguments, flags and return codes as
+ * for the real routines.
+ * ------------------------------------------------------------------------- */
+int kblasCsyrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuFloatComplex alpha, const cuFloatComplex **A_array, int lda,
+                     const cuFloatComplex beta, cuFloatComplex **B_array, int ldb, int batchCount);
+int kblasZsyrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuDoubleComplex alpha, const cuDoubleComplex **A_array, int lda,
+                     const cuDoubleComplex beta, cuDoubleComplex **B_array, int ldb, int batchCount);
+int kblasCsyrk_batch_strided(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                             const cuFloatComplex alpha, const cuFloatComplex *A, int lda, long strideA,
+                             const cuFloatComplex beta, cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblasZsyrk_batch_strided(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                             const cuDoubleComplex alpha, const cuDoubleComplex *A, int lda, long strideA,
+                             const cuDoubleComplex beta, cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblasCtrsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const cuFloatComplex alpha,
+                     const cuFloatComplex **A_array, int lda, cuFloatComplex **B_array, int ldb, int batchCount);
+int kblasZtrsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const cuDoubleComplex alpha,
+                     const cuDoubleComplex **A_array, int lda, cuDoubleComplex **B_array, int ldb, int batchCount);
+int kblasCtrsm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const cuFloatComplex alpha,
+                             const cuFloatComplex *A, int lda, long strideA,
+                             cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblasZtrsm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const cuDoubleComplex alpha,
+                             const cuDoubleComplex *A, int lda, long strideA,
+                             cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblasCtrmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const cuFloatComplex alpha,
+                     const cuFloatComplex **A_array, int lda, cuFloatComplex **B_array, int ldb, int batchCount);
+int kblasZtrmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                     const int m, const int n, const cuDoubleComplex alpha,
+                     const cuDoubleComplex **A_array, int lda, cuDoubleComplex **B_array, int ldb, int batchCount);
+int kblasCtrmm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const cuFloatComplex alpha,
+                             const cuFloatComplex *A, int lda, long strideA,
+                             cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblasZtrmm_batch_strided(kblasHandle_t handle, char side, char uplo, char trans, char diag,
+                             const int m, const int n, const cuDoubleComplex alpha,
+                             const cuDoubleComplex *A, int lda, long strideA,
+                             cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblasCpotrf_batch(kblasHandle_t handle, char uplo, const int n,
+                      cuFloatComplex **A_array, int lda, int batchCount, int *info_array);
+int kblasZpotrf_batch(kblasHandle_t handle, char uplo, const int n,
+                      cuDoubleComplex **A_array, int lda, int batchCount, int *info_array);
+int kblasCpotrf_batch_strided(kblasHandle_t handle, char uplo, const int n,
+                              cuFloatComplex *A, int lda, long strideA, int batchCount, int *info_array);
+int kblasZpotrf_batch_strided(kblasHandle_t handle, char uplo, const int n,
+                              cuDoubleComplex *A, int lda, long strideA, int batchCount, int *info_array);
+int kblasCpotrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuFloatComplex **A_array, int lda, cuFloatComplex **B_array, int ldb, int batchCount);
+int kblasZpotrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuDoubleComplex **A_array, int lda, cuDoubleComplex **B_array, int ldb, int batchCount);
+int kblasCpotrs_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                              const cuFloatComplex *A, int lda, long strideA,
+                              cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblasZpotrs_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                              const cuDoubleComplex *A, int lda, long strideA,
+                              cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblasCposv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     cuFloatComplex **A_array, int lda, cuFloatComplex **B_array, int ldb,
+                     int batchCount, int *info_array);
+int kblasZposv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                     cuDoubleComplex **A_array, int lda, cuDoubleComplex **B_array, int ldb,
+                     int batchCount, int *info_array);
+int kblasCposv_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                             cuFloatComplex *A, int lda, long strideA, cuFloatComplex *B, int ldb, long strideB,
+                             int batchCount, int *info_array);
+int kblasZposv_batch_strided(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                             cuDoubleComplex *A, int lda, long strideA, cuDoubleComplex *B, int ldb, long strideB,
+                             int batchCount, int *info_array);
+int kblasCtrtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuFloatComplex **A_array,
+                      int lda, int batchCount, int *info_array);
+int kblasZtrtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuDoubleComplex **A_array,
+                      int lda, int batchCount, int *info_array);
+int kblasCtrtri_batch_strided(kblasHandle_t handle, char uplo, char diag, const int n, cuFloatComplex *A,
+                              int lda, long strideA, int batchCount, int *info_array);
+int kblasZtrtri_batch_strided(kblasHandle_t handle, char uplo, char diag, const int n, cuDoubleComplex *A,
+                              int lda, long strideA, int batchCount, int *info_array);
+int kblasClauum_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasZlauum_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasClauum_batch_strided(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasZlauum_batch_strided(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasCpotri_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasZpotri_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A_array, int lda,
+                      int batchCount, int *info_array);
+int kblasCpotri_batch_strided(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasZpotri_batch_strided(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda,
+                              long strideA, int batchCount, int *info_array);
+int kblasCpoti_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A_array, int lda,
+                     int batchCount, int *info_array);
+int kblasZpoti_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A_array, int lda,
+                     int batchCount, int *info_array);
+int kblasCpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda,
+                             long strideA, int batchCount, int *info_array);
+int kblasZpoti_batch_strided(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda,
+                             long strideA, int batchCount, int *info_array);
+int kblasCgemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuFloatComplex alpha, const cuFloatComplex **A, int lda,
+                     const cuFloatComplex **B, int ldb, const cuFloatComplex beta, cuFloatComplex **C, int ldc,
+                     int batchCount);
+int kblasZgemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuDoubleComplex alpha, const cuDoubleComplex **A, int lda,
+                     const cuDoubleComplex **B, int ldb, const cuDoubleComplex beta, cuDoubleComplex **C, int ldc,
+                     int batchCount);
+int kblasCgemm_batch_strided(kblasHandle_t handle, char transA, char transB, const int m,
+                             const int n, const int k, const cuFloatComplex alpha, const cuFloatComplex *A,
+                             int lda, long strideA, const cuFloatComplex *B, int ldb, long strideB,
+                             const cuFloatComplex beta, cuFloatComplex *C, int ldc, long strideC, int batchCount);
+int kblasZgemm_batch_strided(kblasHandle_t handle, char transA, char transB, const int m,
+                             const int n, const int k, const cuDoubleComplex alpha, const cuDoubleComplex *A,
+                             int lda, long strideA, const cuDoubleComplex *B, int ldb, long strideB,
+                             const cuDoubleComplex beta, cuDoubleComplex *C, int ldc, long strideC, int batchCount);
+int kblasCgemm_vbatch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                      int max_m, int max_n, int max_k, const cuFloatComplex alpha, const cuFloatComplex **A,
+                      int *lda, const cuFloatComplex **B, int *ldb, const cuFloatComplex beta, cuFloatComplex **C,
+                      int *ldc, int batchCount);
+int kblasZgemm_vbatch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                      int max_m, int max_n, int max_k, const cuDoubleComplex alpha, const cuDoubleComplex **A,
+                      int *lda, const cuDoubleComplex **B, int *ldb, const cuDoubleComplex beta, cuDoubleComplex **C,
+                      int *ldc, int batchCount);
+int kblasCsyrk_vbatch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                      int max_n, const cuFloatComplex alpha, const cuFloatComplex **A, int *lda,
+                      const cuFloatComplex beta, cuFloatComplex **B, int *ldb, int batchCount);
+int kblasZsyrk_vbatch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
+                      int max_n, const cuDoubleComplex alpha, const cuDoubleComplex **A, int *lda,
+                      const cuDoubleComplex beta, cuDoubleComplex **B, int *ldb, int batchCount);
+int kblasCtrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                      int *n, int max_m, int max_n, const cuFloatComplex alpha, const cuFloatComplex **A,
+                      int *lda, cuFloatComplex **B, int *ldb, int batchCount);
+int kblasZtrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
+                      int *n, int max_m, int max_n, const cuDoubleComplex alpha, const cuDoubleComplex **A,
+                      int *lda, cuDoubleComplex **B, int *ldb, int batchCount);
+
 /* ===========================================================================
  * Extensions with no reference counterpart.
  * ========================================================================= */
@@ -358,59 +510,61 @@ int kblasGetDeviceStatus(kblasHandle_t handle);
 #endif
 
 #ifdef __cplusplus
-/* C++ overloads, reference include/kblas_batch.h:1393-1453 and siblings. */
-int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float **A_array, int lda,
-                      int batchCount, int *info_array);
-int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double **A_array, int lda,
-                      int batchCount, int *info_array);
-int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda,
-                      long strideA, int batchCount, int *info_array);
-int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda,
-                      long strideA, int batchCount, int *info_array);
+/* C++ overloads, reference include/kblas_batch.h:82-245 (GEMM), 493-576 (SYRK),
+ * 794-891 (TRSM), 1119-1177 (TRMM), 1396-1452 (POTRF), 1627-2729 (TRTRI / LAUUM /
+ * POTRI / POTI), 2094-2152 (POTRS), 2790-2855 (POSV); S, D, C, Z. */
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda, long strideA,
+                      int batchCount, int *info);
 int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                      const float **A_array, int lda, float **B_array, int ldb, int batchCount);
+                      const float **A, int lda, float **B, int ldb, int batchCount);
 int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                      const double **A_array, int lda, double **B_array, int ldb, int batchCount);
+                      const double **A, int lda, double **B, int ldb, int batchCount);
 int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
                       const float *A, int lda, long strideA, float *B, int ldb, long strideB,
                       int batchCount);
 int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
                       const double *A, int lda, long strideA, double *B, int ldb, long strideB,
                       int batchCount);
-int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                     float **A, int lda, float **B, int ldb, int batchCount, int *info_array);
-int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                     double **A, int lda, double **B, int ldb, int batchCount, int *info_array);
-int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                     float *A, int lda, long strideA, float *B, int ldb, long strideB,
-                     int batchCount, int *info_array);
-int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
-                     double *A, int lda, long strideA, double *B, int ldb, long strideB,
-                     int batchCount, int *info_array);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const float alpha, const float **A, int lda,
-                     float **B, int ldb, int batchCount);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const double alpha, const double **A, int lda,
-                     double **B, int ldb, int batchCount);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const float alpha, const float *A, int lda,
-                     long strideA, float *B, int ldb, long strideB, int batchCount);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const double alpha, const double *A, int lda,
-                     long strideA, double *B, int ldb, long strideB, int batchCount);
-int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const float alpha, const float **A, int lda,
-                     float **B, int ldb, int batchCount);
-int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const double alpha, const double **A, int lda,
-                     double **B, int ldb, int batchCount);
-int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const float alpha, const float *A, int lda,
-                     long strideA, float *B, int ldb, long strideB, int batchCount);
-int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag,
-                     const int m, const int n, const double alpha, const double *A, int lda,
-                     long strideA, double *B, int ldb, long strideB, int batchCount);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, float **A,
+                     int lda, float **B, int ldb, int batchCount, int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, double **A,
+                     int lda, double **B, int ldb, int batchCount, int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, float *A,
+                     int lda, long strideA, float *B, int ldb, long strideB, int batchCount,
+                     int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, double *A,
+                     int lda, long strideA, double *B, int ldb, long strideB, int batchCount,
+                     int *info);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float **A, int lda, float **B, int ldb,
+                     int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double **A, int lda, double **B,
+                     int ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float *A, int lda, long strideA,
+                     float *B, int ldb, long strideB, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double *A, int lda, long strideA,
+                     double *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float **A, int lda, float **B, int ldb,
+                     int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double **A, int lda, double **B,
+                     int ldb, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const float alpha, const float *A, int lda, long strideA,
+                     float *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const double alpha, const double *A, int lda, long strideA,
+                     double *B, int ldb, long strideB, int batchCount);
 int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
                      const float alpha, const float **A, int lda, const float beta, float **B,
                      int ldb, int batchCount);
@@ -427,9 +581,8 @@ int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m
                      const int k, const float alpha, const float **A, int lda, const float **B,
                      int ldb, const float beta, float **C, int ldc, int batchCount);
 int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
-                     const int k, const double alpha, const double **A, int lda,
-                     const double **B, int ldb, const double beta, double **C, int ldc,
-                     int batchCount);
+                     const int k, const double alpha, const double **A, int lda, const double **B,
+                     int ldb, const double beta, double **C, int ldc, int batchCount);
 int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
                      const int k, const float alpha, const float *A, int lda, long strideA,
                      const float *B, int ldb, long strideB, const float beta, float *C, int ldc,
@@ -446,18 +599,180 @@ int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, int *m, int
                      int max_m, int max_n, int max_k, const double alpha, const double **A,
                      int *lda, const double **B, int *ldb, const double beta, double **C,
                      int *ldc, int batchCount);
-int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
-                     int max_n, float alpha, float **A, int *lda, float beta, float **B, int *ldb,
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     float alpha, float **A, int *lda, float beta, float **B, int *ldb,
                      int batchCount);
-int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m,
-                     int max_n, double alpha, double **A, int *lda, double beta, double **B,
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     double alpha, double **A, int *lda, double beta, double **B, int *ldb,
+                     int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, float alpha, float **A, int *lda, float **B, int *ldb,
+                     int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, double alpha, double **A, int *lda, double **B,
                      int *ldb, int batchCount);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
-                     int *n, int max_m, int max_n, float alpha, float **A, int *lda, float **B,
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potrf_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuFloatComplex **A, int lda, cuFloatComplex **B, int ldb, int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuDoubleComplex **A, int lda, cuDoubleComplex **B, int ldb, int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuFloatComplex *A, int lda, long strideA, cuFloatComplex *B, int ldb, long strideB,
+                      int batchCount);
+int kblas_potrs_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n,
+                      const cuDoubleComplex *A, int lda, long strideA, cuDoubleComplex *B, int ldb, long strideB,
+                      int batchCount);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, cuFloatComplex **A,
+                     int lda, cuFloatComplex **B, int ldb, int batchCount, int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, cuDoubleComplex **A,
+                     int lda, cuDoubleComplex **B, int ldb, int batchCount, int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, cuFloatComplex *A,
+                     int lda, long strideA, cuFloatComplex *B, int ldb, long strideB, int batchCount,
+                     int *info);
+int kblas_posv_batch(kblasHandle_t handle, char side, char uplo, const int m, const int n, cuDoubleComplex *A,
+                     int lda, long strideA, cuDoubleComplex *B, int ldb, long strideB, int batchCount,
+                     int *info);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuFloatComplex alpha, const cuFloatComplex **A, int lda, cuFloatComplex **B,
+                     int ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuDoubleComplex alpha, const cuDoubleComplex **A, int lda, cuDoubleComplex **B,
+                     int ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuFloatComplex alpha, const cuFloatComplex *A, int lda, long strideA,
+                     cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuDoubleComplex alpha, const cuDoubleComplex *A, int lda, long strideA,
+                     cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuFloatComplex alpha, const cuFloatComplex **A, int lda, cuFloatComplex **B,
+                     int ldb, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuDoubleComplex alpha, const cuDoubleComplex **A, int lda, cuDoubleComplex **B,
+                     int ldb, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuFloatComplex alpha, const cuFloatComplex *A, int lda, long strideA,
+                     cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblas_trmm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, const int m,
+                     const int n, const cuDoubleComplex alpha, const cuDoubleComplex *A, int lda, long strideA,
+                     cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuFloatComplex alpha, const cuFloatComplex **A, int lda, const cuFloatComplex beta, cuFloatComplex **B,
+                     int ldb, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuDoubleComplex alpha, const cuDoubleComplex **A, int lda, const cuDoubleComplex beta, cuDoubleComplex **B,
+                     int ldb, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuFloatComplex alpha, const cuFloatComplex *A, int lda, long strideA,
+                     const cuFloatComplex beta, cuFloatComplex *B, int ldb, long strideB, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, const int m, const int n,
+                     const cuDoubleComplex alpha, const cuDoubleComplex *A, int lda, long strideA,
+                     const cuDoubleComplex beta, cuDoubleComplex *B, int ldb, long strideB, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuFloatComplex alpha, const cuFloatComplex **A, int lda, const cuFloatComplex **B,
+                     int ldb, const cuFloatComplex beta, cuFloatComplex **C, int ldc, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuDoubleComplex alpha, const cuDoubleComplex **A, int lda, const cuDoubleComplex **B,
+                     int ldb, const cuDoubleComplex beta, cuDoubleComplex **C, int ldc, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuFloatComplex alpha, const cuFloatComplex *A, int lda, long strideA,
+                     const cuFloatComplex *B, int ldb, long strideB, const cuFloatComplex beta, cuFloatComplex *C,
+                     int ldc, long strideC, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, const int m, const int n,
+                     const int k, const cuDoubleComplex alpha, const cuDoubleComplex *A, int lda, long strideA,
+                     const cuDoubleComplex *B, int ldb, long strideB, const cuDoubleComplex beta, cuDoubleComplex *C,
+                     int ldc, long strideC, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const cuFloatComplex alpha, const cuFloatComplex **A,
+                     int *lda, const cuFloatComplex **B, int *ldb, const cuFloatComplex beta, cuFloatComplex **C,
+                     int *ldc, int batchCount);
+int kblas_gemm_batch(kblasHandle_t handle, char transA, char transB, int *m, int *n, int *k,
+                     int max_m, int max_n, int max_k, const cuDoubleComplex alpha, const cuDoubleComplex **A,
+                     int *lda, const cuDoubleComplex **B, int *ldb, const cuDoubleComplex beta, cuDoubleComplex **C,
+                     int *ldc, int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     cuFloatComplex alpha, cuFloatComplex **A, int *lda, cuFloatComplex beta, cuFloatComplex **B, int *ldb,
+                     int batchCount);
+int kblas_syrk_batch(kblasHandle_t handle, char uplo, char trans, int *m, int *n, int max_m, int max_n,
+                     cuDoubleComplex alpha, cuDoubleComplex **A, int *lda, cuDoubleComplex beta, cuDoubleComplex **B, int *ldb,
+                     int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, cuFloatComplex alpha, cuFloatComplex **A, int *lda, cuFloatComplex **B,
                      int *ldb, int batchCount);
-int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m,
-                     int *n, int max_m, int max_n, double alpha, double **A, int *lda,
-                     double **B, int *ldb, int batchCount);
+int kblas_trsm_batch(kblasHandle_t handle, char side, char uplo, char trans, char diag, int *m, int *n,
+                     int max_m, int max_n, cuDoubleComplex alpha, cuDoubleComplex **A, int *lda, cuDoubleComplex **B,
+                     int *ldb, int batchCount);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, float **A, int lda,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, float *A, int lda,
+                      long strideA, int batchCount, int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, float **A, int lda, int batchCount,
+                      int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, float *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, double **A, int lda,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, double *A, int lda,
+                      long strideA, int batchCount, int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, double **A, int lda, int batchCount,
+                      int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, double *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuFloatComplex **A, int lda,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuFloatComplex *A, int lda,
+                      long strideA, int batchCount, int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, cuFloatComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuDoubleComplex **A, int lda,
+                      int batchCount, int *info);
+int kblas_trtri_batch(kblasHandle_t handle, char uplo, char diag, const int n, cuDoubleComplex *A, int lda,
+                      long strideA, int batchCount, int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_lauum_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_potri_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex **A, int lda, int batchCount,
+                      int *info);
+int kblas_poti_batch(kblasHandle_t handle, char uplo, const int n, cuDoubleComplex *A, int lda, long strideA,
+                      int batchCount, int *info);
 #endif /* __cplusplus */
 
 #endif /* KBLAS_GB300_BATCH_H */

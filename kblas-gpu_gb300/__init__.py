@@ -103,7 +103,7 @@ _SIG = {
     "kblas_syrk_batch_nonuniform_wsquery": (None, [P]),
     "kblas_trsm_batch_nonuniform_wsquery": (None, [P]),
 }
-for _x in ("S", "D"):
+for _x in ("S", "D", "C", "Z"):
     _SIG.update({
         f"kblas{_x}trtri_batch": (I, [P, CH, CH, I, P, I, I, P]),
         f"kblas{_x}trtri_batch_strided": (I, [P, CH, CH, I, P, I, L, I, P]),
@@ -113,7 +113,17 @@ for _x in ("S", "D"):
             f"kblas{_x}{_op}_batch": (I, [P, CH, I, P, I, I, P]),
             f"kblas{_x}{_op}_batch_strided": (I, [P, CH, I, P, I, L, I, P]),
         })
-for _x, _R in (("S", F), ("D", D)):
+class ComplexF(C.Structure):
+    """cuFloatComplex by value."""
+    _fields_ = [("x", C.c_float), ("y", C.c_float)]
+
+
+class ComplexD(C.Structure):
+    """cuDoubleComplex by value."""
+    _fields_ = [("x", C.c_double), ("y", C.c_double)]
+
+
+for _x, _R in (("S", F), ("D", D), ("C", ComplexF), ("Z", ComplexD)):
     _SIG.update({
         f"kblas{_x}syrk_batch": (I, [P, CH, CH, I, I, _R, P, I, _R, P, I, I]),
         f"kblas{_x}syrk_batch_strided": (I, [P, CH, CH, I, I, _R, P, I, L, _R, P, I, L, I]),
@@ -217,7 +227,15 @@ class Handle:
 
     # ---- generic call by C name: self.call("kblasDposv_batch_strided", ...) ----
     def call(self, name: str, *args) -> int:
+        f = getattr(lib(), name)
+        types = list(f.argtypes[1:]) if f.argtypes else []
+        types += [None] * (len(args) - len(types))
         conv = []
-        for a in args:
-            conv.append(_b(a) if isinstance(a, str) else a)
-        return getattr(lib(), name)(self.ptr, *conv)
+        for a, t in zip(args, types):
+            if isinstance(a, str):
+                a = _b(a)
+            elif t in (ComplexF, ComplexD):
+                z = complex(a)
+                a = t(z.real, z.imag)
+            conv.append(a)
+        return f(self.ptr, *conv)

@@ -92,4 +92,14 @@ __device__ __forceinline__ bool is_pos_pivot(T d) {
   return d > T(0);  // false for NaN
 }
 
+// sqrt of an accepted pivot, correctly rounded (FP32 through FP64).
+__device__ __forceinline__ double pivot_sqrt(double d) { return sqrt(d); }
+__device__ __forceinline__ float pivot_sqrt(float d) { return (float)sqrt((double)d); }
+
+__device__ __forceinline__ double shfl_xor_t(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float shfl_xor_t(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+
 }  // namespace kgb
+
+// the complex value type and its overloads of the helpers above
+#include "cplx.cuh"

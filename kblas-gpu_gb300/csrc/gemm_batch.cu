@@ -19,6 +19,8 @@
 // a matrix with m <= 0 or n <= 0 is skipped.
 #include <stdio.h>
 
+#include <cuComplex.h>
+
 #include "gemm_tile.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
@@ -217,5 +219,46 @@ int kblasDsyrk_vbatch(kblasHandle_t h, char uplo, char trans, int *m, int *n, in
   return syrk_vbatch<double>(h, uplo, trans, m, n, max_m, max_n, alpha, A, lda, beta, B, ldb,
                              batchCount);
 }
+
+// Complex precisions (op = transpose, as the reference's KBLAS_Trans):
+// uniform GEMM (reference kblas{C,Z}gemm_batch[_strided]) and the
+// variable-size GEMM / SYRK (its complex non-uniform overloads).
+#define KGB_GEMM_CPLX(X, API, T)                                                                   \
+  int kblas##X##gemm_batch(kblasHandle_t h, char transA, char transB, const int m, const int n,    \
+                           const int k, const API alpha, const API **A, int lda, const API **B,    \
+                           int ldb, const API beta, API **C, int ldc, int batchCount) {            \
+    return gemm_array<T>(h, transA, transB, m, n, k, T(alpha.x, alpha.y),                          \
+                         reinterpret_cast<const T **>(A), lda, reinterpret_cast<const T **>(B),    \
+                         ldb, T(beta.x, beta.y), reinterpret_cast<T **>(C), ldc, batchCount);      \
+  }                                                                                                \
+  int kblas##X##gemm_batch_strided(kblasHandle_t h, char transA, char transB, const int m,         \
+                                   const int n, const int k, const API alpha, const API *A,        \
+                                   int lda, long strideA, const API *B, int ldb, long strideB,     \
+                                   const API beta, API *C, int ldc, long strideC,                  \
+                                   int batchCount) {                                               \
+    return gemm_strided<T>(h, transA, transB, m, n, k, T(alpha.x, alpha.y),                        \
+                           reinterpret_cast<const T *>(A), lda, strideA,                           \
+                           reinterpret_cast<const T *>(B), ldb, strideB, T(beta.x, beta.y),        \
+                           reinterpret_cast<T *>(C), ldc, strideC, batchCount);                    \
+  }                                                                                                \
+  int kblas##X##gemm_vbatch(kblasHandle_t h, char transA, char transB, int *m, int *n, int *k,     \
+                            int max_m, int max_n, int max_k, const API alpha, const API **A,       \
+                            int *lda, const API **B, int *ldb, const API beta, API **C, int *ldc,  \
+                            int batchCount) {                                                      \
+    return gemm_vbatch<T>(h, transA, transB, m, n, k, max_m, max_n, max_k, T(alpha.x, alpha.y),    \
+                          reinterpret_cast<const T **>(A), lda, reinterpret_cast<const T **>(B),   \
+                          ldb, T(beta.x, beta.y), reinterpret_cast<T **>(C), ldc, batchCount);     \
+  }                                                                                                \
+  int kblas##X##syrk_vbatch(kblasHandle_t h, char uplo, char trans, int *m, int *n, int max_m,     \
+                            int max_n, const API alpha, const API **A, int *lda, const API beta,   \
+                            API **B, int *ldb, int batchCount) {                                   \
+    return syrk_vbatch<T>(h, uplo, trans, m, n, max_m, max_n, T(alpha.x, alpha.y),                 \
+                          reinterpret_cast<const T **>(A), lda, T(beta.x, beta.y),                 \
+                          reinterpret_cast<T **>(B), ldb, batchCount);                             \
+  }
+
+KGB_GEMM_CPLX(C, cuFloatComplex, cxf)
+KGB_GEMM_CPLX(Z, cuDoubleComplex, cxd)
+#undef KGB_GEMM_CPLX
 
 }  // extern "C"

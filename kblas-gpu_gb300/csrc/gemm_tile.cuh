@@ -59,6 +59,20 @@ __device__ __forceinline__ void ld4(const double *p, double (&v)[4]) {
   v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
 }
 
+__device__ __forceinline__ void ld4(const cx<float> *p, cx<float> (&v)[4]) {
+  const float4 q0 = *reinterpret_cast<const float4 *>(p);
+  const float4 q1 = *reinterpret_cast<const float4 *>(p + 2);
+  v[0] = cx<float>(q0.x, q0.y); v[1] = cx<float>(q0.z, q0.w);
+  v[2] = cx<float>(q1.x, q1.y); v[3] = cx<float>(q1.z, q1.w);
+}
+__device__ __forceinline__ void ld4(const cx<double> *p, cx<double> (&v)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const double2 q = *reinterpret_cast<const double2 *>(p + i);
+    v[i] = cx<double>(q.x, q.y);
+  }
+}
+
 // One C tile. Every thread of the CTA calls it (it holds barriers). BLAS
 // semantics: op(A), op(B) are not read when alpha == 0 or k == 0, C is not
 // read when beta == 0.

@@ -21,6 +21,8 @@
 //   POTRI  TRTRI then LAUUM;  POTI  a left-looking Cholesky, then POTRI.
 #include <stdio.h>
 
+#include <cuComplex.h>
+
 #include "device_util.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
@@ -97,11 +99,11 @@ __device__ int blk_potrf(T *M, int ld, int n, int *s_flag)
     if (threadIdx.x < 32) {
       T s = T(0);
       for (int k = threadIdx.x; k < j; k += 32) s += el(M, ld, j, k) * el(M, ld, j, k);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      for (int o = 16; o > 0; o >>= 1) s += shfl_xor_t(s, o);
       if (threadIdx.x == 0) {
         const T d = el(M, ld, j, j) - s;
-        const bool ok = d > T(0);  // false for NaN
-        el(M, ld, j, j) = ok ? (T)sqrt((double)d) : d;
+        const bool ok = is_pos_pivot(d);  // real: d > 0, false for NaN
+        el(M, ld, j, j) = ok ? pivot_sqrt(d) : d;
         *s_flag = ok ? 0 : j + 1;
       }
     }
@@ -254,46 +256,48 @@ void kblas_potri_batch_strided_wsquery(kblasHandle_t, const int, int) {}
 void kblas_poti_batch_wsquery(kblasHandle_t, const int, int) {}
 void kblas_poti_batch_strided_wsquery(kblasHandle_t, const int, int) {}
 
-#define KGB_INV_ENTRIES(X, T)                                                                   \
-  int kblas##X##trtri_batch(kblasHandle_t h, char uplo, char diag, const int n, T **A, int lda, \
+#define KGB_INV_ENTRIES(X, API, T)                                                                   \
+  int kblas##X##trtri_batch(kblasHandle_t h, char uplo, char diag, const int n, API **A, int lda, \
                             int batchCount, int *info) {                                        \
-    return inv_array<T, INV_TRTRI>(h, uplo, diag, n, A, lda, batchCount, info, "TRTRI");         \
+    return inv_array<T, INV_TRTRI>(h, uplo, diag, n, reinterpret_cast<T **>(A), lda, batchCount, info, "TRTRI");         \
   }                                                                                             \
-  int kblas##X##trtri_batch_strided(kblasHandle_t h, char uplo, char diag, const int n, T *A,   \
+  int kblas##X##trtri_batch_strided(kblasHandle_t h, char uplo, char diag, const int n, API *A,   \
                                     int lda, long strideA, int batchCount, int *info) {         \
-    return inv_strided<T, INV_TRTRI>(h, uplo, diag, n, A, lda, strideA, batchCount, info,       \
+    return inv_strided<T, INV_TRTRI>(h, uplo, diag, n, reinterpret_cast<T *>(A), lda, strideA, batchCount, info,       \
                                      "TRTRI");                                                  \
   }                                                                                             \
-  int kblas##X##lauum_batch(kblasHandle_t h, char uplo, const int n, T **A, int lda,             \
+  int kblas##X##lauum_batch(kblasHandle_t h, char uplo, const int n, API **A, int lda,             \
                             int batchCount, int *info) {                                        \
-    return inv_array<T, INV_LAUUM>(h, uplo, 'N', n, A, lda, batchCount, info, "LAUUM");          \
+    return inv_array<T, INV_LAUUM>(h, uplo, 'N', n, reinterpret_cast<T **>(A), lda, batchCount, info, "LAUUM");          \
   }                                                                                             \
-  int kblas##X##lauum_batch_strided(kblasHandle_t h, char uplo, const int n, T *A, int lda,     \
+  int kblas##X##lauum_batch_strided(kblasHandle_t h, char uplo, const int n, API *A, int lda,     \
                                     long strideA, int batchCount, int *info) {                  \
-    return inv_strided<T, INV_LAUUM>(h, uplo, 'N', n, A, lda, strideA, batchCount, info,        \
+    return inv_strided<T, INV_LAUUM>(h, uplo, 'N', n, reinterpret_cast<T *>(A), lda, strideA, batchCount, info,        \
                                      "LAUUM");                                                  \
   }                                                                                             \
-  int kblas##X##potri_batch(kblasHandle_t h, char uplo, const int n, T **A, int lda,             \
+  int kblas##X##potri_batch(kblasHandle_t h, char uplo, const int n, API **A, int lda,             \
                             int batchCount, int *info) {                                        \
-    return inv_array<T, INV_POTRI>(h, uplo, 'N', n, A, lda, batchCount, info, "POTRI");          \
+    return inv_array<T, INV_POTRI>(h, uplo, 'N', n, reinterpret_cast<T **>(A), lda, batchCount, info, "POTRI");          \
   }                                                                                             \
-  int kblas##X##potri_batch_strided(kblasHandle_t h, char uplo, const int n, T *A, int lda,     \
+  int kblas##X##potri_batch_strided(kblasHandle_t h, char uplo, const int n, API *A, int lda,     \
                                     long strideA, int batchCount, int *info) {                  \
-    return inv_strided<T, INV_POTRI>(h, uplo, 'N', n, A, lda, strideA, batchCount, info,        \
+    return inv_strided<T, INV_POTRI>(h, uplo, 'N', n, reinterpret_cast<T *>(A), lda, strideA, batchCount, info,        \
                                      "POTRI");                                                  \
   }                                                                                             \
-  int kblas##X##poti_batch(kblasHandle_t h, char uplo, const int n, T **A, int lda,              \
+  int kblas##X##poti_batch(kblasHandle_t h, char uplo, const int n, API **A, int lda,              \
                            int batchCount, int *info) {                                         \
-    return inv_array<T, INV_POTI>(h, uplo, 'N', n, A, lda, batchCount, info, "POTI");            \
+    return inv_array<T, INV_POTI>(h, uplo, 'N', n, reinterpret_cast<T **>(A), lda, batchCount, info, "POTI");            \
   }                                                                                             \
-  int kblas##X##poti_batch_strided(kblasHandle_t h, char uplo, const int n, T *A, int lda,      \
+  int kblas##X##poti_batch_strided(kblasHandle_t h, char uplo, const int n, API *A, int lda,      \
                                    long strideA, int batchCount, int *info) {                   \
-    return inv_strided<T, INV_POTI>(h, uplo, 'N', n, A, lda, strideA, batchCount, info,         \
+    return inv_strided<T, INV_POTI>(h, uplo, 'N', n, reinterpret_cast<T *>(A), lda, strideA, batchCount, info,         \
                                     "POTI");                                                    \
   }
 
-KGB_INV_ENTRIES(S, float)
-KGB_INV_ENTRIES(D, double)
+KGB_INV_ENTRIES(S, float, float)
+KGB_INV_ENTRIES(D, double, double)
+KGB_INV_ENTRIES(C, cuFloatComplex, cxf)
+KGB_INV_ENTRIES(Z, cuDoubleComplex, cxd)
 #undef KGB_INV_ENTRIES
 
 }  // extern "C"

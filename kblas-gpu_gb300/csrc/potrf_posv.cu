@@ -12,6 +12,8 @@
 #include <stdio.h>
 #include <type_traits>
 
+#include <cuComplex.h>
+
 #include "chol_kernels.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
@@ -62,7 +64,7 @@ template <typename T, int MODE, class AccA, class AccB>
 static int launch_chol(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
                        long long batch, int *info) {
   if (n <= 32) {
-    switch (team_size_for(n, sizeof(T) == 8)) {
+    switch (team_size_for(n, std::is_same<T, double>::value)) {
       case 2: return launch_team<T, 2, MODE>(h, n, m, A, lda, B, ldb, batch, info);
       case 4: return launch_team<T, 4, MODE>(h, n, m, A, lda, B, ldb, batch, info);
       default: return launch_team<T, 8, MODE>(h, n, m, A, lda, B, ldb, batch, info);
@@ -91,7 +93,7 @@ int fp64_uniform_persistent(KBlasHandle *h, int op, int m, int n, SysArgs sys, i
 template <typename T, class AccA, class AccB>
 static int try_persistent(KBlasHandle *h, int op, int m, int n, AccA A, int lda, AccB B, int ldb,
                           int batch, int *info) {
-  if (sizeof(T) != 8 || n <= 32 || n > PC_MAX_N) return KBLAS_InsufficientWorkspace;
+  if (!std::is_same<T, double>::value || n <= 32 || n > PC_MAX_N) return KBLAS_InsufficientWorkspace;
   SysArgs s{};
   if constexpr (std::is_same<AccA, Strided<T>>::value) {
     s.mode = 0;
@@ -339,5 +341,43 @@ int kblasDposv_batch_strided(kblasHandle_t h, char side, char uplo, const int m,
   return posv_strided<double>(h, side, uplo, m, n, A, lda, strideA, B, ldb, strideB, batchCount,
                               info);
 }
+
+// Complex precisions (the reference's kblas{C,Z}{potrf,potrs,posv}_batch[_strided],
+// complex-symmetric: A = L L^T, nothing conjugated).
+#define KGB_CHOL_CPLX(X, API, T)                                                                  \
+  int kblas##X##potrf_batch(kblasHandle_t h, char uplo, const int n, API **A, int lda,            \
+                            int batchCount, int *info) {                                          \
+    return potrf_array<T>(h, uplo, n, reinterpret_cast<T **>(A), lda, batchCount, info);          \
+  }                                                                                               \
+  int kblas##X##potrf_batch_strided(kblasHandle_t h, char uplo, const int n, API *A, int lda,     \
+                                    long strideA, int batchCount, int *info) {                    \
+    return potrf_strided<T>(h, uplo, n, reinterpret_cast<T *>(A), lda, strideA, batchCount, info); \
+  }                                                                                               \
+  int kblas##X##potrs_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,      \
+                            const API **A, int lda, API **B, int ldb, int batchCount) {           \
+    return potrs_array<T>(h, side, uplo, m, n, reinterpret_cast<const T **>(A), lda,              \
+                          reinterpret_cast<T **>(B), ldb, batchCount);                            \
+  }                                                                                               \
+  int kblas##X##potrs_batch_strided(kblasHandle_t h, char side, char uplo, const int m,           \
+                                    const int n, const API *A, int lda, long strideA, API *B,     \
+                                    int ldb, long strideB, int batchCount) {                      \
+    return potrs_strided<T>(h, side, uplo, m, n, reinterpret_cast<const T *>(A), lda, strideA,    \
+                            reinterpret_cast<T *>(B), ldb, strideB, batchCount);                  \
+  }                                                                                               \
+  int kblas##X##posv_batch(kblasHandle_t h, char side, char uplo, const int m, const int n,       \
+                           API **A, int lda, API **B, int ldb, int batchCount, int *info) {       \
+    return posv_array<T>(h, side, uplo, m, n, reinterpret_cast<T **>(A), lda,                     \
+                         reinterpret_cast<T **>(B), ldb, batchCount, info);                       \
+  }                                                                                               \
+  int kblas##X##posv_batch_strided(kblasHandle_t h, char side, char uplo, const int m,            \
+                                   const int n, API *A, int lda, long strideA, API *B, int ldb,   \
+                                   long strideB, int batchCount, int *info) {                     \
+    return posv_strided<T>(h, side, uplo, m, n, reinterpret_cast<T *>(A), lda, strideA,           \
+                           reinterpret_cast<T *>(B), ldb, strideB, batchCount, info);             \
+  }
+
+KGB_CHOL_CPLX(C, cuFloatComplex, cxf)
+KGB_CHOL_CPLX(Z, cuDoubleComplex, cxd)
+#undef KGB_CHOL_CPLX
 
 }  // extern "C"

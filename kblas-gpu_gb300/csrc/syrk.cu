@@ -11,6 +11,8 @@
 // time, and a 2 x 2 register tile of C per thread.
 #include <stdio.h>
 
+#include <cuComplex.h>
+
 #include "device_util.cuh"
 #include "gemm_tile.cuh"
 #include "kblas_internal.h"
@@ -175,5 +177,28 @@ int kblasDsyrk_batch_strided(kblasHandle_t h, char uplo, char trans, const int m
   return syrk_strided<double>(h, uplo, trans, m, n, alpha, A, lda, strideA, beta, B, ldb, strideB,
                               batchCount);
 }
+
+// Complex precisions: C := alpha op(A) op(A)^T + beta C (complex-symmetric,
+// the reference's kblas{C,Z}syrk_batch; no conjugation).
+#define KGB_SYRK_CPLX(X, API, T)                                                                   \
+  int kblas##X##syrk_batch(kblasHandle_t h, char uplo, char trans, const int m, const int n,       \
+                           const API alpha, const API **A, int lda, const API beta, API **B,       \
+                           int ldb, int batchCount) {                                              \
+    return syrk_array<T>(h, uplo, trans, m, n, T(alpha.x, alpha.y),                                \
+                         reinterpret_cast<const T **>(A), lda, T(beta.x, beta.y),                  \
+                         reinterpret_cast<T **>(B), ldb, batchCount);                              \
+  }                                                                                                \
+  int kblas##X##syrk_batch_strided(kblasHandle_t h, char uplo, char trans, const int m,            \
+                                   const int n, const API alpha, const API *A, int lda,            \
+                                   long strideA, const API beta, API *B, int ldb, long strideB,    \
+                                   int batchCount) {                                               \
+    return syrk_strided<T>(h, uplo, trans, m, n, T(alpha.x, alpha.y),                              \
+                           reinterpret_cast<const T *>(A), lda, strideA, T(beta.x, beta.y),        \
+                           reinterpret_cast<T *>(B), ldb, strideB, batchCount);                    \
+  }
+
+KGB_SYRK_CPLX(C, cuFloatComplex, cxf)
+KGB_SYRK_CPLX(Z, cuDoubleComplex, cxd)
+#undef KGB_SYRK_CPLX
 
 }  // extern "C"

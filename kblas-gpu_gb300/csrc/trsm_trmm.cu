@@ -23,6 +23,8 @@
 // layout is sized for the largest triangle.
 #include <stdio.h>
 
+#include <cuComplex.h>
+
 #include "device_util.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
@@ -257,6 +259,18 @@ template int trsm_batch_internal<float, PtrArr<float>, PtrArr<float>>(
 template int trsm_batch_internal<double, PtrArr<double>, PtrArr<double>>(
     KBlasHandle *, char, char, char, char, int, int, double, PtrArr<double>, int, PtrArr<double>,
     int, long long, const int *);
+template int trsm_batch_internal<cxf, Strided<cxf>, Strided<cxf>>(
+    KBlasHandle *, char, char, char, char, int, int, cxf, Strided<cxf>, int, Strided<cxf>, int,
+    long long, const int *);
+template int trsm_batch_internal<cxd, Strided<cxd>, Strided<cxd>>(
+    KBlasHandle *, char, char, char, char, int, int, cxd, Strided<cxd>, int, Strided<cxd>, int,
+    long long, const int *);
+template int trsm_batch_internal<cxf, PtrArr<cxf>, PtrArr<cxf>>(
+    KBlasHandle *, char, char, char, char, int, int, cxf, PtrArr<cxf>, int, PtrArr<cxf>, int,
+    long long, const int *);
+template int trsm_batch_internal<cxd, PtrArr<cxd>, PtrArr<cxd>>(
+    KBlasHandle *, char, char, char, char, int, int, cxd, PtrArr<cxd>, int, PtrArr<cxd>, int,
+    long long, const int *);
 
 static inline int check_tri(KBlasHandle *h, char side, char uplo, char trans, char diag, int m,
                             int n, int lda, int ldb, int batch) {
@@ -425,5 +439,55 @@ int kblasDtrsm_vbatch(kblasHandle_t h, char side, char uplo, char trans, char di
   return trsm_vbatch<double>(h, side, uplo, trans, diag, m, n, max_m, max_n, alpha, A, lda, B,
                              ldb, batchCount);
 }
+
+// Complex precisions (op = transpose, never conjugate-transpose, as the
+// reference's KBLAS_Trans; every side / uplo / trans / diag).
+#define KGB_TRI_CPLX(X, API, T)                                                                    \
+  int kblas##X##trsm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag,           \
+                           const int m, const int n, const API alpha, const API **A, int lda,      \
+                           API **B, int ldb, int batchCount) {                                     \
+    return tri_array<T, 0>(h, side, uplo, trans, diag, m, n, T(alpha.x, alpha.y),                  \
+                           reinterpret_cast<const T **>(A), lda, reinterpret_cast<T **>(B), ldb,   \
+                           batchCount);                                                            \
+  }                                                                                                \
+  int kblas##X##trsm_batch_strided(kblasHandle_t h, char side, char uplo, char trans, char diag,   \
+                                   const int m, const int n, const API alpha, const API *A,        \
+                                   int lda, long strideA, API *B, int ldb, long strideB,           \
+                                   int batchCount) {                                               \
+    return tri_strided<T, 0>(h, side, uplo, trans, diag, m, n, T(alpha.x, alpha.y),                \
+                             reinterpret_cast<const T *>(A), lda, strideA,                         \
+                             reinterpret_cast<T *>(B), ldb, strideB, batchCount);                  \
+  }                                                                                                \
+  int kblas##X##trmm_batch(kblasHandle_t h, char side, char uplo, char trans, char diag,           \
+                           const int m, const int n, const API alpha, const API **A, int lda,      \
+                           API **B, int ldb, int batchCount) {                                     \
+    return tri_array<T, 1>(h, side, uplo, trans, diag, m, n, T(alpha.x, alpha.y),                  \
+                           reinterpret_cast<const T **>(A), lda, reinterpret_cast<T **>(B), ldb,   \
+                           batchCount);                                                            \
+  }                                                                                                \
+  int kblas##X##trmm_batch_strided(kblasHandle_t h, char side, char uplo, char trans, char diag,   \
+                                   const int m, const int n, const API alpha, const API *A,        \
+                                   int lda, long strideA, API *B, int ldb, long strideB,           \
+                                   int batchCount) {                                               \
+    return tri_strided<T, 1>(h, side, uplo, trans, diag, m, n, T(alpha.x, alpha.y),                \
+                             reinterpret_cast<const T *>(A), lda, strideA,                         \
+                             reinterpret_cast<T *>(B), ldb, strideB, batchCount);                  \
+  }
+
+#define KGB_TRSM_VB_CPLX(X, API, T)                                                                \
+  int kblas##X##trsm_vbatch(kblasHandle_t h, char side, char uplo, char trans, char diag, int *m,  \
+                            int *n, int max_m, int max_n, const API alpha, const API **A,          \
+                            int *lda, API **B, int *ldb, int batchCount) {                         \
+    return trsm_vbatch<T>(h, side, uplo, trans, diag, m, n, max_m, max_n, T(alpha.x, alpha.y),     \
+                          reinterpret_cast<const T **>(A), lda, reinterpret_cast<T **>(B), ldb,    \
+                          batchCount);                                                             \
+  }
+KGB_TRSM_VB_CPLX(C, cuFloatComplex, cxf)
+KGB_TRSM_VB_CPLX(Z, cuDoubleComplex, cxd)
+#undef KGB_TRSM_VB_CPLX
+
+KGB_TRI_CPLX(C, cuFloatComplex, cxf)
+KGB_TRI_CPLX(Z, cuDoubleComplex, cxd)
+#undef KGB_TRI_CPLX
 
 }  // extern "C"

@@ -35,6 +35,29 @@
 #undef REAL
 #undef PFX
 
+/* complex-symmetric instantiations (C99 complex: the same layout as
+ * cuDoubleComplex / cuFloatComplex and numpy complex128 / complex64) */
+#include <complex.h>
+#define ORC_PIVOT_BAD(d) ((d) == 0 || !isfinite(creal(d)) || !isfinite(cimag(d)))
+#define ORC_SQRT(d) csqrt(d)
+#define REAL double _Complex
+#define PFX z
+#include "oracle_impl.h"
+#undef REAL
+#undef PFX
+#undef ORC_PIVOT_BAD
+#undef ORC_SQRT
+
+#define ORC_PIVOT_BAD(d) ((d) == 0 || !isfinite(crealf(d)) || !isfinite(cimagf(d)))
+#define ORC_SQRT(d) csqrtf(d)
+#define REAL float _Complex
+#define PFX c
+#include "oracle_impl.h"
+#undef REAL
+#undef PFX
+#undef ORC_PIVOT_BAD
+#undef ORC_SQRT
+
 #define AT(M, ld, i, j) (M)[(size_t)(i) + (size_t)(j) * (size_t)(ld)]
 
 /* A(i,j) of a symmetric matrix given by its lower triangle. */

@@ -47,7 +47,7 @@ def lib():
             L = C.CDLL(LIB_PATH)
             P = C.c_void_p
             I, Lg, D, F, Ch = C.c_int, C.c_long, C.c_double, C.c_float, C.c_char
-            for pfx, R in (("d", D), ("s", F)):
+            for pfx, R in (("d", D), ("s", F), ("z", _Z), ("c", _CF)):
                 getattr(L, f"oracle_{pfx}potrf").argtypes = [I, P, I]
                 getattr(L, f"oracle_{pfx}potrf").restype = I
                 getattr(L, f"oracle_{pfx}potrs").argtypes = [I, I, P, I, P, I]
@@ -83,6 +83,27 @@ def lib():
     return _lib
 
 
+class _Z(C.Structure):
+    """double _Complex passed by value (same ABI class as two doubles)."""
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class _CF(C.Structure):
+    """float _Complex passed by value."""
+    _fields_ = [("re", C.c_float), ("im", C.c_float)]
+
+
+def _scal(a: np.ndarray, v):
+    """A scalar argument (alpha / beta) in the type of the array's routines."""
+    if a.dtype == np.complex128:
+        v = complex(v)
+        return _Z(v.real, v.imag)
+    if a.dtype == np.complex64:
+        v = complex(v)
+        return _CF(v.real, v.imag)
+    return v
+
+
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
 
@@ -92,6 +113,10 @@ def _pfx(a: np.ndarray) -> str:
         return "d"
     if a.dtype == np.float32:
         return "s"
+    if a.dtype == np.complex128:
+        return "z"
+    if a.dtype == np.complex64:
+        return "c"
     raise TypeError(a.dtype)
 
 
@@ -140,7 +165,7 @@ def trsm_batch(side, uplo, trans, diag, m, n, alpha, A, B, nthreads=None):
     batch, ncol, lda = A.shape
     _, ncolb, ldb = B.shape
     getattr(lib(), f"oracle_{_pfx(A)}trsm_batch")(_b(side), _b(uplo), _b(trans), _b(diag), m, n,
-                                                  alpha, _p(A), lda, ncol * lda, _p(B), ldb,
+                                                  _scal(A, alpha), _p(A), lda, ncol * lda, _p(B), ldb,
                                                   ncolb * ldb, batch, nthreads or nthreads_default())
 
 
@@ -148,15 +173,16 @@ def trmm_batch(side, uplo, trans, diag, m, n, alpha, A, B, nthreads=None):
     batch, ncol, lda = A.shape
     _, ncolb, ldb = B.shape
     getattr(lib(), f"oracle_{_pfx(A)}trmm_batch")(_b(side), _b(uplo), _b(trans), _b(diag), m, n,
-                                                  alpha, _p(A), lda, ncol * lda, _p(B), ldb,
+                                                  _scal(A, alpha), _p(A), lda, ncol * lda, _p(B), ldb,
                                                   ncolb * ldb, batch, nthreads or nthreads_default())
 
 
 def syrk_batch(uplo, trans, m, k, alpha, A, beta, Cm, nthreads=None):
     batch, ncol, lda = A.shape
     _, ncolc, ldc = Cm.shape
-    getattr(lib(), f"oracle_{_pfx(A)}syrk_batch")(_b(uplo), _b(trans), m, k, alpha, _p(A), lda,
-                                                  ncol * lda, beta, _p(Cm), ldc, ncolc * ldc,
+    getattr(lib(), f"oracle_{_pfx(A)}syrk_batch")(_b(uplo), _b(trans), m, k, _scal(A, alpha), _p(A),
+                                                  lda, ncol * lda, _scal(A, beta), _p(Cm), ldc,
+                                                  ncolc * ldc,
                                                   batch, nthreads or nthreads_default())
 
 
@@ -165,8 +191,9 @@ def gemm_batch(transA, transB, m, n, k, alpha, A, B, beta, Cm, nthreads=None):
     batch, ncol, lda = A.shape
     _, ncolb, ldb = B.shape
     _, ncolc, ldc = Cm.shape
-    getattr(lib(), f"oracle_{_pfx(A)}gemm_batch")(_b(transA), _b(transB), m, n, k, alpha, _p(A),
-                                                  lda, ncol * lda, _p(B), ldb, ncolb * ldb, beta,
+    getattr(lib(), f"oracle_{_pfx(A)}gemm_batch")(_b(transA), _b(transB), m, n, k, _scal(A, alpha),
+                                                  _p(A), lda, ncol * lda, _p(B), ldb, ncolb * ldb,
+                                                  _scal(A, beta),
                                                   _p(Cm), ldc, ncolc * ldc, batch,
                                                   nthreads or nthreads_default())
 

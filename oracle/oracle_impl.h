@@ -1,7 +1,8 @@
 /*
  * oracle_impl.h -- precision-generic body of the CPU oracle (TEST
  * INFRASTRUCTURE ONLY: included twice by kblas_oracle.c, once with
- * REAL = double and once with REAL = float).
+ * REAL = double / float, and for the complex routines with REAL = double
+ * _Complex / float _Complex: the same loops, nothing conjugated).
  *
  * The reference library has no CPU implementation of the batched path; its
  * tests check every routine against host LAPACK/BLAS looped over the batch
@@ -21,6 +22,16 @@
 
 #define AT(M, ld, i, j) (M)[(size_t)(i) + (size_t)(j) * (size_t)(ld)]
 
+/* Pivot test and square root of the factorization: real types fail on a
+ * pivot <= 0 or NaN (LAPACK); the complex instantiation (complex-symmetric,
+ * A = L L^T without conjugation, the reference's complex batch routines)
+ * fails on a zero or non-finite pivot and takes the principal root. */
+#ifndef ORC_PIVOT_BAD
+#define ORC_PIVOT_BAD(d) (!((d) > (REAL)0))  /* also catches NaN */
+#define ORC_SQRT(d) ((REAL)sqrt((double)(d)))
+#define ORC_DEFAULT_PIVOT 1
+#endif
+
 /* LAPACK xPOTF2, lower: column-by-column dot-product (left-looking) Cholesky.
  * info = j (1-based) for the first pivot that is <= 0 or NaN; A(j,j) then
  * holds that pivot value and the columns after it are untouched, as in
@@ -31,11 +42,11 @@ int ORC(potrf)(int n, REAL *A, int lda)
     for (int j = 0; j < n; j++) {
         REAL ajj = AT(A, lda, j, j);
         for (int k = 0; k < j; k++) ajj -= AT(A, lda, j, k) * AT(A, lda, j, k);
-        if (!(ajj > (REAL)0)) {  /* also catches NaN */
+        if (ORC_PIVOT_BAD(ajj)) {
             AT(A, lda, j, j) = ajj;
             return j + 1;
         }
-        ajj = (REAL)sqrt((double)ajj);
+        ajj = ORC_SQRT(ajj);
         AT(A, lda, j, j) = ajj;
         for (int i = j + 1; i < n; i++) {
             REAL s = AT(A, lda, i, j);
@@ -378,3 +389,9 @@ void ORC(posv_vbatch)(const int *m, const int *n, REAL **A, const int *lda, REAL
 #undef ORC
 #undef ORC_CAT
 #undef ORC_CAT_
+
+#ifdef ORC_DEFAULT_PIVOT
+#undef ORC_PIVOT_BAD
+#undef ORC_SQRT
+#undef ORC_DEFAULT_PIVOT
+#endif

@@ -187,6 +187,42 @@ def main():
         c, info = lapack.dpotrf(a, lower=0, clean=0)
         out["dpotrfu_bad_n40_A"] = a
         out["dpotrfu_bad_n40_info"] = np.int32(info)
+    # complex BLAS (no conjugation: op = transpose, SYRK = A A^T), the forms
+    # the reference's C / Z batch routines compute; a fifth stream
+    r5 = rng(2028, 4)
+    for dt, name in ((np.complex128, "z"), (np.complex64, "c")):
+        gemm, syrk, trsm, trmm = (getattr(blas, name + f) for f in ("gemm", "syrk", "trsm", "trmm"))
+
+        def cn(*shape):
+            return (r5.standard_normal(shape) + 1j * r5.standard_normal(shape)).astype(dt)
+        for (m, n, k) in ((5, 7, 3), (33, 17, 40)):
+            for ta in "NT":
+                for tb in "NT":
+                    a = cn(*((m, k) if ta == "N" else (k, m)))
+                    b = cn(*((k, n) if tb == "N" else (n, k)))
+                    c0 = cn(m, n)
+                    res = gemm(1.5 - 0.5j, a, b, beta=0.25 + 1j, c=c0, trans_a=int(ta == "T"),
+                               trans_b=int(tb == "T"))
+                    key = f"{name}gemm_{ta}{tb}_m{m}_n{n}_k{k}"
+                    out.update({key + "_A": a, key + "_B": b, key + "_C": c0, key + "_R": res})
+        for (m, k) in ((6, 4), (40, 23)):
+            for trans in "NT":
+                a = cn(*((m, k) if trans == "N" else (k, m)))
+                c0 = cn(m, m)
+                c0 = np.tril(c0) + np.tril(c0, -1).T
+                res = syrk(-1.0, a, beta=1.0, c=c0, trans=int(trans == "T"), lower=1)
+                key = f"{name}syrk_{trans}_m{m}_k{k}"
+                out.update({key + "_A": a, key + "_C": c0, key + "_R": np.tril(res)})
+        for (m, n) in ((9, 4), (33, 12)):
+            L = np.tril(cn(m, m)) / np.sqrt(m) + np.diag(r5.uniform(1, 2, m) + 0.5j)
+            L = L.astype(dt)
+            b = cn(m, n)
+            for trans in "NT":
+                key = f"{name}tri_{trans}_m{m}_n{n}"
+                out[key + "_L"] = L
+                out[key + "_B"] = b
+                out[key + "_trsm"] = trsm(0.5 + 0.5j, L, b, lower=1, trans_a=int(trans == "T"))
+                out[key + "_trmm"] = trmm(0.5 + 0.5j, L, b, lower=1, trans_a=int(trans == "T"))
     path = os.path.join(HERE, "lapack_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, len(out), "arrays", os.path.getsize(path), "bytes")

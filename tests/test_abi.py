@@ -24,7 +24,8 @@ def declared_functions():
 
 
 CXX_OVERLOADS = {"kblas_potrf_batch", "kblas_potrs_batch", "kblas_posv_batch", "kblas_trsm_batch",
-                 "kblas_trmm_batch", "kblas_syrk_batch", "kblas_gemm_batch"}
+                 "kblas_trmm_batch", "kblas_syrk_batch", "kblas_gemm_batch", "kblas_trtri_batch",
+                 "kblas_lauum_batch", "kblas_potri_batch", "kblas_poti_batch"}
 
 
 @pytest.fixture(scope="module")
@@ -56,10 +57,10 @@ def test_exports_every_declared_symbol(built):
 def test_cxx_overloads_exported(built):
     out = subprocess.run(["nm", "-D", "--defined-only", built.LIB_PATH], capture_output=True,
                          text=True).stdout
-    # uniform S/D x (pointer array, strided); GEMM, SYRK, TRSM add S/D variable-size
-    counts = {"kblas_potrf_batch": 4, "kblas_potrs_batch": 4, "kblas_posv_batch": 4,
-              "kblas_trsm_batch": 6, "kblas_trmm_batch": 4, "kblas_syrk_batch": 6,
-              "kblas_gemm_batch": 6}
+    # the reference's sets: S, D, C, Z x (pointer array, strided); GEMM, SYRK and
+    # TRSM add the four variable-size forms (100 overloads in all)
+    counts = {b: 8 for b in CXX_OVERLOADS}
+    counts.update({"kblas_trsm_batch": 12, "kblas_syrk_batch": 12, "kblas_gemm_batch": 12})
     for base, want in counts.items():
         mangled = [l for l in out.splitlines() if f"{len(base)}{base}" in l]
         assert len(mangled) == want, (base, mangled)

@@ -171,6 +171,83 @@ def test_potrf_uplo_and_side_l_potrs_vs_lapack(golden, orc, pfx):
         assert info[0] == int(golden["dpotrfu_bad_n40_info"]) == 18
 
 
+CEPS = {"z": 2.0 ** -53, "c": 2.0 ** -24}
+
+
+@pytest.mark.parametrize("pfx", ["z", "c"])
+def test_complex_blas_vs_blas(golden, orc, pfx):
+    """Complex GEMM / SYRK / TRSM / TRMM (transpose, never conjugate) against
+    BLAS zgemm / zsyrk / ztrsm / ztrmm (and the c routines)."""
+    dt = np.complex128 if pfx == "z" else np.complex64
+    e = CEPS[pfx]
+    for c in keys(golden, rf"{pfx}gemm_(\w\w_m\d+_n\d+_k\d+)_A"):
+        tt, ms, ns, ks = c.split("_")
+        m, n, k = int(ms[1:]), int(ns[1:]), int(ks[1:])
+        g = {x: golden[f"{pfx}gemm_{c}_{x}"] for x in "ABCR"}
+        cm = colmajor(g["C"], dt)
+        orc.gemm_batch(tt[0], tt[1], m, n, k, 1.5 - 0.5j, colmajor(g["A"], dt), colmajor(g["B"], dt),
+                       0.25 + 1j, cm, nthreads=1)
+        scale = 2 * k * np.abs(g["A"]).max() * np.abs(g["B"]).max() + 2 * np.abs(g["C"]).max()
+        assert np.abs(cm[0].T - g["R"]).max() <= 20 * k * e * scale, c
+    for c in keys(golden, rf"{pfx}syrk_(\w_m\d+_k\d+)_A"):
+        trans, ms, ks = c.split("_")
+        m, k = int(ms[1:]), int(ks[1:])
+        cm = colmajor(golden[f"{pfx}syrk_{c}_C"], dt)
+        orc.syrk_batch("L", trans, m, k, -1.0, colmajor(golden[f"{pfx}syrk_{c}_A"], dt), 1.0, cm,
+                       nthreads=1)
+        scale = 2 * k * np.abs(golden[f"{pfx}syrk_{c}_A"]).max() ** 2 + np.abs(golden[f"{pfx}syrk_{c}_C"]).max()
+        assert np.abs(np.tril(cm[0].T) - golden[f"{pfx}syrk_{c}_R"]).max() <= 20 * k * e * scale, c
+    for c in keys(golden, rf"{pfx}tri_(\w_m\d+_n\d+)_L"):
+        trans, ms, ns = c.split("_")
+        m, n = int(ms[1:]), int(ns[1:])
+        L = colmajor(golden[f"{pfx}tri_{c}_L"], dt)
+        for op, fn in (("trsm", orc.trsm_batch), ("trmm", orc.trmm_batch)):
+            b = colmajor(golden[f"{pfx}tri_{c}_B"], dt)
+            fn("L", "L", trans, "N", m, n, 0.5 + 0.5j, L, b, nthreads=1)
+            ref = golden[f"{pfx}tri_{c}_{op}"]
+            assert np.abs(b[0].T - ref).max() <= 100 * m * e * np.abs(ref).max(), (c, op)
+
+
+@pytest.mark.parametrize("pfx", ["z", "c"])
+def test_complex_symmetric_cholesky_properties(orc, pfx):
+    """Complex POTRF / POTRS / POSV / inversion have no LAPACK counterpart
+    (LAPACK's xPOTRF is Hermitian); the complex-symmetric forms are pinned by
+    their defining identities on the reference's test recipe (random, diagonal
+    += n + n i, symmetrized): L L^T = A, X A = B, A inv(A) = I, and on
+    real-valued complex input they equal the real routines."""
+    dt = np.complex128 if pfx == "z" else np.complex64
+    e = CEPS[pfx]
+    rng = np.random.default_rng(5)
+    for n in (1, 7, 30, 65):
+        g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        g[np.arange(n), np.arange(n)] += n + 1j * n
+        a = np.tril(g) + np.tril(g, -1).T
+        A = colmajor(a, dt)
+        L = A.copy()
+        assert orc.potrf_batch(L, n, nthreads=1)[0] == 0
+        Lr = np.tril(L[0].T).astype(np.complex128)
+        assert np.abs(Lr @ Lr.T - a).max() <= 30 * n * e * np.abs(a).max(), n
+        b = rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))
+        B = colmajor(b, dt)
+        X = B.copy()
+        orc.potrs_batch(L, X, 3, n, nthreads=1)
+        x = X[0].T.astype(np.complex128)
+        assert np.abs(x @ a - b).max() <= 100 * n * e * np.abs(a).max() * np.abs(x).max(), n
+        Ai = A.copy()
+        assert orc.poti_batch(Ai, n, nthreads=1)[0] == 0
+        li = np.tril(Ai[0].T).astype(np.complex128)
+        inv = li + np.tril(li, -1).T
+        assert np.abs(inv @ a - np.eye(n)).max() <= 300 * n * e * np.abs(a).max() * np.abs(inv).max()
+        # real-valued complex input: the same numbers as the real factorization
+        ar = a.real + n * np.eye(n)
+        Lc = colmajor(ar, dt)
+        Lre = colmajor(ar, np.float64 if pfx == "z" else np.float32)
+        orc.potrf_batch(Lc, n, nthreads=1)
+        orc.potrf_batch(Lre, n, nthreads=1)
+        assert np.abs(np.tril(Lc[0].T).imag).max() == 0
+        assert np.abs(np.tril(Lc[0].T).real - np.tril(Lre[0].T)).max() <= 10 * n * e * np.abs(ar).max()
+
+
 def test_backward_error_detects_wrong_solution(orc):
     """A planted mistake in the solution must blow the backward error up."""
     rng = np.random.default_rng(1)
