@@ -601,6 +601,105 @@ __device__ void team_llt_solve_panel(const Team &t, const PanelLayout &L, const 
   }
 }
 
+// Y := L^{-T} L^{-1} Y for nr right-hand sides at once (y + q * n, q < nr,
+// 2 <= nr < nwarps), on an INV factor, by the whole team: one sweep over the
+// panels with the barriers of a single solve, every factor element loaded
+// once per sweep step for all right-hand sides. Per right-hand side the
+// arithmetic and its order are those of team_llt_solve_panel<T, true>, so
+// the results are identical to nr solves in turn. The diagonal blocks run on
+// warps 0..nr-1 in parallel, one right-hand side each. red: nr * nwarps * 32
+// elements of team-shared scratch.
+template <typename T, int NRMAX>
+__device__ void team_llt_solve_panel_inv_multi(const Team &t, const PanelLayout &L, const T *Ps,
+                                               T *y, int nr, T *red)
+{
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  const int n = L.n;
+  for (int p = 0; p < L.np; p++) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    if (w < nr) {
+      // y_J := L_JJ^{-1} y_J for right-hand side w
+      T *yq = y + (size_t)w * n;
+      T v0 = T(0), v1 = T(0);
+      if (lane < jb) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          if (k <= lane && k < jb) v0 += Pp[lane + k * ld] * yq[J + k];
+          if (k + 1 <= lane && k + 1 < jb) v1 += Pp[lane + (k + 1) * ld] * yq[J + k + 1];
+        }
+      }
+      __syncwarp();
+      if (lane < jb) yq[J + lane] = v0 + v1;
+    }
+    t.sync();
+    for (int i = jb + t.tid; i < n - J; i += t.nt) {
+      T s0[NRMAX], s1[NRMAX];
+#pragma unroll
+      for (int q = 0; q < NRMAX; q++) s0[q] = s1[q] = T(0);
+#pragma unroll 4
+      for (int c = 0; c < jb; c += 2) {
+        const T a0 = Pp[i + c * ld];
+        const T a1 = (c + 1 < jb) ? Pp[i + (c + 1) * ld] : T(0);
+#pragma unroll
+        for (int q = 0; q < NRMAX; q++) {
+          if (q < nr) {
+            const T *yq = y + (size_t)q * n;
+            s0[q] += a0 * yq[J + c];
+            if (c + 1 < jb) s1[q] += a1 * yq[J + c + 1];
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NRMAX; q++)
+        if (q < nr) y[(size_t)q * n + J + i] -= s0[q] + s1[q];
+    }
+    t.sync();
+  }
+  for (int p = L.np - 1; p >= 0; p--) {
+    const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+    const T *Pp = Ps + L.base(p);
+    // partials of right-hand side q: warp w sums its row chunks (lane = row)
+    for (int q = 0; q < nr; q++) {
+      const T *yq = y + (size_t)q * n;
+      T acc[32];
+#pragma unroll
+      for (int c = 0; c < 32; c++) acc[c] = T(0);
+      for (int i0 = jb + w * 32; i0 < n - J; i0 += nw * 32) {
+        const int i = i0 + lane;
+        const T yi = (i < n - J) ? yq[J + i] : T(0);
+        const T *row = Pp + min(i, ld - 1);
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+          if (c < jb) acc[c] += row[(size_t)c * ld] * yi;
+      }
+      const T part = warp_transpose_sum32<T>(acc);
+      red[((size_t)q * nw + w) * 32 + lane] = part;
+    }
+    t.sync();
+    if (w < nr) {
+      // x_J := L_JJ^{-T} (y_J - partials) for right-hand side w
+      T *yq = y + (size_t)w * n;
+      const T *rq = red + (size_t)w * nw * 32;
+      T sv = (lane < jb) ? yq[J + lane] : T(0);
+      for (int q = 0; q < nw; q++) sv -= rq[q * 32 + lane];
+      if (lane < jb) yq[J + lane] = sv;
+      __syncwarp();
+      T v0 = T(0), v1 = T(0);
+      if (lane < jb) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+          if (k >= lane && k < jb) v0 += Pp[lane + k * ld] * yq[J + k];
+          if (k + 1 >= lane && k + 1 < jb) v1 += Pp[lane + (k + 1) * ld] * yq[J + k + 1];
+        }
+      }
+      __syncwarp();
+      if (lane < jb) yq[J + lane] = v0 + v1;
+    }
+    t.sync();
+  }
+}
+
 // Stage the lower triangle of A (FP64, column-major, lda) into panel storage
 // of type T (SCALE: FP32 a_ij * 2^(sh[i] + sh[j]), converted on the integer
 // pipe, see f64_to_f32_scaled; sh = -e of the row scale 2^-e). One thread per

@@ -346,15 +346,21 @@ static __device__ int panel_fp64_posv(const Team &t, int n, int m, int r_from, d
 
 // FP32 solves of nr right-hand sides (ys, stride n) with an INV factor: with
 // at least as many right-hand sides as warps, one warp per right-hand side
-// (no team barriers); otherwise the whole team on each in turn (a single
-// warp is latency-bound on one solve).
+// (no team barriers); with fewer (but several), the whole team on all of
+// them in one sweep when `wide` (wide_elems floats of team-shared scratch)
+// holds the nr * nwarps * 32 partial sums (the sweep runs right-hand side q's
+// diagonal blocks on warp q, so it needs nr < nwarps); otherwise the whole
+// team on each in turn (a single warp is latency-bound on one solve).
 static __device__ void team_solve_rhs(const Team &t, const PanelLayout &L, const float *Ps,
-                                      const float *rinv, float *ys, int nr, float *red)
+                                      const float *rinv, float *ys, int nr, float *red,
+                                      float *wide, size_t wide_elems)
 {
   const int nw = t.nwarps();
   if (nw > 1 && nr >= nw) {
     for (int q = t.warp(); q < nr; q += nw) warp_llt_solve_inv<float>(L, Ps, ys + (size_t)q * L.n);
     t.sync();
+  } else if (nr >= 2 && nr < nw && nr <= PC_MR && (size_t)nr * nw * 32 <= wide_elems) {
+    team_llt_solve_panel_inv_multi<float, PC_MR>(t, L, Ps, ys, nr, wide);
   } else {
     for (int q = 0; q < nr; q++) team_llt_solve_panel<float, true>(t, L, Ps, rinv, ys + (size_t)q * L.n, red, true);
   }
@@ -479,7 +485,8 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
       for (int i = t.tid; i < n; i += t.nt)
         ys[q * n + i] = f64_to_f32_scaled(B[(size_t)(r0 + q) + (size_t)i * ldb], sh[i]);
     t.sync();
-    team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red));
+    team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red),
+                   reinterpret_cast<float *>(colsum), (size_t)nw * n * 2);
     for (int q = 0; q < nr; q++)
       for (int i = t.tid; i < n; i += t.nt) x[q * n + i] = (double)(ys[q * n + i] * scl[i]);
     t.sync();
@@ -533,7 +540,8 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
       for (int q = 0; q < nr; q++)
         for (int i = t.tid; i < n; i += t.nt) ys[q * n + i] = f64_to_f32_scaled(r[q * n + i], sh[i]);
       t.sync();
-      team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red));
+      team_solve_rhs(t, L, Ps, rinv, ys, nr, reinterpret_cast<float *>(red),
+                   reinterpret_cast<float *>(colsum), (size_t)nw * n * 2);
       for (int q = 0; q < nr; q++)
         for (int i = t.tid; i < n; i += t.nt) x[q * n + i] += (double)(ys[q * n + i] * scl[i]);
       t.sync();

@@ -86,6 +86,29 @@ def test_mixed_illconditioned_cond_1e2_to_1e8(gpu, handle, kb, wl, orc):
     assert (it[cond < 1e4] >= 0).all()
 
 
+@pytest.mark.parametrize("n", [150, 300])
+@pytest.mark.parametrize("m", [2, 3, 5, 7])
+def test_mixed_panel_path_several_rhs_covariance(gpu, handle, kb, wl, orc, n, m):
+    """Panel path with 4- and 8-warp teams and 2..4 right-hand sides per
+    sweep (the sweep that solves them all at once), on squared-exponential
+    covariances (nugget 1e-4, cond up to ~1e6), which take several refinement
+    steps: every system meets the bar and stays close to the FP64 solution."""
+    batch = 6
+    a = wl.sqexp_cov(batch, n, seed=n + m)
+    b = wl.rhs_rows(batch, m, n, seed=5 * m + 1)
+    A, X, info, it = run_uniform_mixed(gpu, kb, handle, a, b, m, n,
+                                       form="strided" if m % 2 else "array")
+    assert (info == 0).all()
+    eta = orc.backward_error_r(a, X, b, m, n)
+    assert eta.max() <= 10 * n * EPS64, eta.max()
+    assert (it >= 1).all(), it  # refinement steps were taken (correction solves ran)
+    assert np.array_equal(A, a)
+    ref_a, ref_b = a.copy(), b.copy()
+    orc.posv_batch(ref_a, ref_b, m, n)
+    fwd = np.abs(X - ref_b).max(axis=(1, 2)) / np.abs(ref_b).max(axis=(1, 2))
+    assert (fwd <= 1e-4).all(), fwd.max()
+
+
 @pytest.mark.parametrize("n", [8, 16, 24])
 def test_mixed_register_path_illconditioned_many_rhs(gpu, handle, kb, wl, orc, n):
     """Register path (several systems share a warp) with cond up to 1e8 and 4
