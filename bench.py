@@ -282,8 +282,12 @@ def accuracy_check(orc, w, torch, sample=1500, seed=0):
                                       [ns[k] for k in good], [Xs[k] for k in good], [1] * len(good),
                                       [Bs[k] for k in good], [1] * len(good))
     ratio = eta / np.array([10 * ns[k] * EPS64 for k in good])
+    # forward error against the oracle's FP64 solution (refB now holds it)
+    fwd = np.array([np.abs(Xs[k] - refB[k]).max() / max(float(np.abs(refB[k]).max()), 1e-300)
+                    for k in good])
     return {"checked": int(len(pick)), "info_exact": info_ok,
             "max_eta_over_10n_eps": float(ratio.max()) if len(ratio) else 0.0,
+            "max_forward_rel_err_vs_oracle": float(fwd.max()) if len(fwd) else 0.0,
             "all_within_bound": bool((ratio <= 1.0).all()),
             "indefinite_checked": int(len(w.indef))}
 
@@ -603,6 +607,12 @@ def run_workload(args):
         eta_m = orc.backward_error_r(a[pick], Xm[pick], b[pick], m, n)
         eta_f = orc.backward_error_r(a[pick], Xf[pick], b[pick], m, n)
         fwd = np.abs(Xm[pick] - Xf[pick]).max(axis=(1, 2)) / np.abs(Xf[pick]).max(axis=(1, 2))
+        # forward errors of both forms against the oracle's FP64 LAPACK-style solution
+        ref_a, ref_b = a[pick].copy(), b[pick].copy()
+        info_o = orc.posv_batch(ref_a, ref_b, m, n)
+        den = np.abs(ref_b).max(axis=(1, 2))
+        fwd_om = np.abs(Xm[pick] - ref_b).max(axis=(1, 2)) / den
+        fwd_of = np.abs(Xf[pick] - ref_b).max(axis=(1, 2)) / den
         flops = batch * (_flops_potrf(n) + 2.0 * m * n * n)
         ex = {"fp64_form": {"value": batch / (ms_f * 1e-3), "unit": "solves/s", "ms_per_step": ms_f,
                             "max_eta_over_10n_eps": float(eta_f.max() / (10 * n * EPS64))},
@@ -611,6 +621,9 @@ def run_workload(args):
                            "max_eta_over_10n_eps": float(eta_m.max() / (10 * n * EPS64)),
                            "all_within_bound": bool((eta_m <= 10 * n * EPS64).all()),
                            "max_forward_rel_diff_vs_fp64": float(fwd.max()),
+                           "max_forward_rel_err_vs_oracle": float(fwd_om.max()),
+                           "fp64_form_max_forward_rel_err_vs_oracle": float(fwd_of.max()),
+                           "oracle_info_equal": bool(np.array_equal(info_o, infom[pick])),
                            "info_equal_to_fp64_form": bool(np.array_equal(infom, infof))},
               "refinement": {"mean_steps": float(itm[itm >= 0].mean()) if (itm >= 0).any() else None,
                              "fallback_systems": int((itm < 0).sum())},
