@@ -155,3 +155,32 @@ int oracle_max_threads(void)
     return 1;
 #endif
 }
+
+/* The reference testers' CPU timing path with the host's own LAPACK
+ * (test_Xposv_batch.cpp:301-326: one LAPACK call per matrix, OpenMP over the
+ * batch): dpotrf + dpotrs through function pointers the caller supplies (an
+ * optimized LAPACK, e.g. the one scipy links; Fortran calling convention,
+ * 32-bit integers), over a variable-size batch with ONE right-hand side per
+ * system stored as a contiguous column of n values (B[b][0..n-1]). info[b]
+ * as dpotrf's; B[b] is solved in place only when info[b] == 0. */
+typedef void (*orc_lapack_dpotrf_fn)(char *, int *, double *, int *, int *);
+typedef void (*orc_lapack_dpotrs_fn)(char *, int *, int *, double *, int *, double *, int *, int *);
+
+void oracle_lapack_dposv1_vbatch(void *potrf, void *potrs, const int *n, double *const *A,
+                                 const int *lda, double *const *B, int batch, int *info,
+                                 int nthreads)
+{
+    const orc_lapack_dpotrf_fn f = (orc_lapack_dpotrf_fn)potrf;
+    const orc_lapack_dpotrs_fn s = (orc_lapack_dpotrs_fn)potrs;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int b = 0; b < batch; b++) {
+        char lo = 'L';
+        int nn = n[b], ld = lda[b], one = 1, inf = 0;
+        if (nn > 0) f(&lo, &nn, A[b], &ld, &inf);
+        if (inf == 0 && nn > 0) {
+            int ldb = nn, inf2 = 0;
+            s(&lo, &nn, &one, A[b], &ld, B[b], &ldb, &inf2);
+        }
+        info[b] = inf;
+    }
+}

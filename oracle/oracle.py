@@ -343,3 +343,81 @@ def backward_error_r_vbatch(ms, ns, As, ldas, Xs, ldxs, Bs, ldbs, nthreads=None)
     lib().oracle_backward_error_r_vbatch(_p(m), _p(n), _p(pa), _p(lda), _p(px), _p(ldx), _p(pb),
                                          _p(ldb), batch, _p(eta), nthreads or nthreads_default())
     return eta
+
+
+# --------------------------------------------------------------------------
+# the host's optimized LAPACK (for the timed CPU baseline)
+# --------------------------------------------------------------------------
+
+_lapack = None
+
+
+def _single_thread_openblas():
+    """Pin the OpenBLAS that scipy loaded to one thread (the batch loop is the
+    parallel level, as in the reference testers). Returns what was done."""
+    import re
+    try:
+        maps = open("/proc/self/maps").read()
+    except OSError:
+        return "unknown"
+    for path in sorted(set(re.findall(r"/\S*scipy\S*openblas\S*\.so\S*", maps))):
+        try:
+            L = C.CDLL(path)
+        except OSError:
+            continue
+        for sym in ("scipy_openblas_set_num_threads", "openblas_set_num_threads"):
+            f = getattr(L, sym, None)
+            if f is not None:
+                f.argtypes = [C.c_int]
+                f(1)
+                return "OpenBLAS pinned to 1 thread (%s)" % sym
+    return "OpenBLAS threads not found"
+
+
+def host_lapack():
+    """(dpotrf, dpotrs, description) of the host LAPACK that scipy links, as
+    raw function addresses, or None when scipy's LAPACK is not importable."""
+    global _lapack
+    with _lock:
+        if _lapack is None:
+            os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")  # if scipy is not loaded yet
+            try:
+                import scipy
+                from scipy.linalg import cython_lapack
+            except Exception:
+                _lapack = False
+                return None
+            api = C.pythonapi
+            api.PyCapsule_GetName.restype = C.c_char_p
+            api.PyCapsule_GetName.argtypes = [C.py_object]
+            api.PyCapsule_GetPointer.restype = C.c_void_p
+            api.PyCapsule_GetPointer.argtypes = [C.py_object, C.c_char_p]
+            ptrs = []
+            for name in ("dpotrf", "dpotrs"):
+                cap = cython_lapack.__pyx_capi__[name]
+                ptrs.append(api.PyCapsule_GetPointer(cap, api.PyCapsule_GetName(cap)))
+            how = _single_thread_openblas()
+            _lapack = (ptrs[0], ptrs[1], "LAPACK dpotrf + dpotrs of scipy %s (%s)" % (scipy.__version__, how))
+    return _lapack or None
+
+
+def lapack_posv1_vbatch(ns, As, ldas, Bs, nthreads=None):
+    """The host LAPACK's dpotrf + dpotrs over a variable-size batch (one
+    right-hand side per system, Bs[b] holding n contiguous values), OpenMP
+    over the batch. Returns info, or None when no host LAPACK is available."""
+    lp = host_lapack()
+    if lp is None:
+        return None
+    L = lib()
+    f = L.oracle_lapack_dposv1_vbatch
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                  C.c_void_p, C.c_int]
+    f.restype = None
+    batch = len(ns)
+    n = np.asarray(ns, dtype=np.int32)
+    lda = np.asarray(ldas, dtype=np.int32)
+    pa = np.array([a.ctypes.data for a in As], dtype=np.uint64)
+    pb = np.array([b.ctypes.data for b in Bs], dtype=np.uint64)
+    info = np.zeros(batch, dtype=np.int32)
+    f(lp[0], lp[1], _p(n), _p(pa), _p(lda), _p(pb), batch, _p(info), nthreads or nthreads_default())
+    return info

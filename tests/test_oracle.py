@@ -319,3 +319,35 @@ def test_trtri_singular_info_and_unchanged(golden, orc, pfx):
         assert info[0] == int(golden[f"{pfx}trtri_sing_n{n}_info"])
         assert np.array_equal(a, a0), "a singular matrix must be left unchanged"
 
+
+
+def test_host_lapack_batch_loop_matches_restatement(orc):
+    """The timed CPU baseline's loop over the host LAPACK (dpotrf + dpotrs
+    through function pointers, OpenMP over the batch) gives the restatement's
+    info codes exactly and the same solutions to rounding, on ragged orders
+    with planted non-SPD systems."""
+    pytest.importorskip("scipy.linalg.cython_lapack")
+    if orc.host_lapack() is None:
+        pytest.skip("no host LAPACK")
+    rng = np.random.default_rng(7)
+    ns = [int(x) for x in rng.integers(1, 140, 400)]
+    As, Bs = [], []
+    for k, n in enumerate(ns):
+        g = rng.standard_normal((n, n))
+        a = np.ascontiguousarray(g @ g.T + n * np.eye(n))
+        if k % 13 == 5:
+            j = k % n
+            a[j, j] = -abs(a[j, j])  # leading minor j+1 not positive definite
+        As.append(a)
+        Bs.append(rng.standard_normal((n, 1)))
+    A1, B1 = [a.copy() for a in As], [b.copy() for b in Bs]
+    A2, B2 = [a.copy() for a in As], [b.copy() for b in Bs]
+    info1 = orc.lapack_posv1_vbatch(ns, A1, ns, B1)
+    info2 = orc.posv_vbatch([1] * len(ns), ns, A2, ns, B2, [1] * len(ns))
+    assert np.array_equal(info1, info2)
+    assert (info1 > 0).sum() == len(range(5, 400, 13))
+    for k, n in enumerate(ns):
+        if info1[k] == 0:
+            assert np.abs(B1[k] - B2[k]).max() <= 1e3 * n * 2.0 ** -53 * np.abs(B2[k]).max()
+        else:
+            assert np.array_equal(B1[k], Bs[k])  # not solved
