@@ -28,6 +28,14 @@ int ensure_device_props(KBlasHandle *h) {
 }
 }  // namespace kgb
 
+// Frees what a partly created handle holds (events, status word) and the handle.
+static void discard_handle(KBlasHandle *h) {
+  if (h->ev_start) cudaEventDestroy(h->ev_start);
+  if (h->ev_end) cudaEventDestroy(h->ev_end);
+  if (h->d_status) cudaFree(h->d_status);
+  delete h;
+}
+
 extern "C" {
 
 int kblasCreate(kblasHandle_t *handle) {
@@ -42,13 +50,13 @@ int kblasCreate(kblasHandle_t *handle) {
   if (cudaEventCreate(&h->ev_start) != cudaSuccess || cudaEventCreate(&h->ev_end) != cudaSuccess ||
       cudaMalloc((void **)&h->d_status, sizeof(int)) != cudaSuccess ||
       cudaMemset(h->d_status, 0, sizeof(int)) != cudaSuccess) {
-    delete h;
+    discard_handle(h);
     *handle = nullptr;
     return KBLAS_CUDA_Error;
   }
   int st = ensure_device_props(h);
   if (st != KBLAS_Success) {
-    delete h;
+    discard_handle(h);
     *handle = nullptr;
     return st;
   }
