@@ -1014,7 +1014,13 @@ def main():
         "gflops_useful": useful / (ms_mixed * 1e-3) / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": read_traffic(),
-                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "note": "algorithmic bytes over the event-timed call. The persistent "
+                             "mixed kernel binds on neither HBM nor tensor cores: it is "
+                             "latency-bound (team barriers, dependent FMA chains, L2 round "
+                             "trips); ncu: DRAM throughput 1.6%, FP64 pipe 23%, FP32 8% "
+                             "(profiles/posv_vbatch_mixed_n8-256.txt). The FP64 form's "
+                             "fraction of the FP64 pipe is in fp64_pipe"},
         "fp64_pipe": {"peak_tflops_measured_live": fp64_peak,
                       "refinement_fp64_tflops": fp64_flops_refine / (ms_mixed * 1e-3) / 1e12,
                       "fp64_form_tflops": useful / (ms_fp64 * 1e-3) / 1e12,
