@@ -384,19 +384,21 @@ def host_lapack():
             try:
                 import scipy
                 from scipy.linalg import cython_lapack
+                api = C.pythonapi
+                api.PyCapsule_GetName.restype = C.c_char_p
+                api.PyCapsule_GetName.argtypes = [C.py_object]
+                api.PyCapsule_GetPointer.restype = C.c_void_p
+                api.PyCapsule_GetPointer.argtypes = [C.py_object, C.c_char_p]
+                ptrs = []
+                for name in ("dpotrf", "dpotrs"):
+                    cap = cython_lapack.__pyx_capi__[name]
+                    ptrs.append(api.PyCapsule_GetPointer(cap, api.PyCapsule_GetName(cap)))
+                if not all(ptrs):
+                    raise RuntimeError("null LAPACK entry point")
+                how = _single_thread_openblas()
             except Exception:
                 _lapack = False
                 return None
-            api = C.pythonapi
-            api.PyCapsule_GetName.restype = C.c_char_p
-            api.PyCapsule_GetName.argtypes = [C.py_object]
-            api.PyCapsule_GetPointer.restype = C.c_void_p
-            api.PyCapsule_GetPointer.argtypes = [C.py_object, C.c_char_p]
-            ptrs = []
-            for name in ("dpotrf", "dpotrs"):
-                cap = cython_lapack.__pyx_capi__[name]
-                ptrs.append(api.PyCapsule_GetPointer(cap, api.PyCapsule_GetName(cap)))
-            how = _single_thread_openblas()
             _lapack = (ptrs[0], ptrs[1], "LAPACK dpotrf + dpotrs of scipy %s (%s)" % (scipy.__version__, how))
     return _lapack or None
 
