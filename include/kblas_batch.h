@@ -488,7 +488,11 @@ int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi
  * device memory, a latency-bound loop where cudaMalloc / cudaFree would stall
  * or fail). Limits: n <= KBLAS_POSV_NOALLOC_MAX_N, else a message and
  * KBLAS_NotSupported; scratch KBLAS_POSV_NOALLOC_SCRATCH_BYTES per device.
- * The first call on a device does set-up: make it before any stream capture.
+ * Every call looks up the array's address in the calling thread's current
+ * context (no address is cached across calls, so the routine stays correct
+ * after cudaDeviceReset and under non-primary contexts); the first call in a
+ * context loads that part of the library's image: make it before any stream
+ * capture.
  * All calls on a device share the array, so calls that overlap in time
  * (different streams without ordering) race and give wrong results; calls in
  * one stream are safe. */

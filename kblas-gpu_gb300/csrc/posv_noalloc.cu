@@ -20,12 +20,13 @@
 //     device; orders n > KBLAS_POSV_NOALLOC_MAX_N (256) are rejected with a
 //     message and KBLAS_NotSupported. The persistent grid is cut, if needed,
 //     to the number of per-CTA slots that fit (n = 256 on 152 SMs: 151);
-//   * the first call on each device does set-up (it looks up the array's
-//     device address, which loads that part of the library's image, and reads
-//     the device's properties): make that first call before any stream
-//     capture begins. The CUDA driver may also grow its own per-context
-//     reservations (module images, local memory) the first time a kernel
-//     runs; that is the driver's, not this routine's;
+//   * every call looks up the array's device address in the current context
+//     (cudaGetSymbolAddress) and reads the device's properties; this stays
+//     correct after cudaDeviceReset and under non-primary contexts. The first
+//     call in a context loads that part of the library's image: make it
+//     before any stream capture begins. The CUDA driver may also grow its own
+//     per-context reservations (module images, local memory) the first time
+//     a kernel runs; that is the driver's, not this routine's;
 //   * every call on a device shares the one array. Its first 256 bytes are
 //     the work counter, which must be zero when the kernel starts: each call
 //     clears it with cudaMemsetAsync on its own stream before its launch. The
@@ -34,7 +35,6 @@
 //     or host threads without ordering between them) race on the counter and
 //     the scratch and give wrong results. Order them: one stream, or events.
 //     Calls in the same stream are ordered and safe.
-#include <mutex>
 #include <stdio.h>
 
 #include "kblas.h"
@@ -54,39 +54,29 @@ namespace {
 // asks for its address, not when the rest of the library is used.
 static __device__ __align__(256) char g_posv_scratch[KBLAS_POSV_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-
+// Looked up on every call, in the calling thread's current context. The
+// address of a __device__ array belongs to the context that loaded the
+// module: caching it per device ordinal would hand a later call a stale
+// address after cudaDeviceReset, or the wrong one when the caller switches to
+// a non-primary context on the same device. Once the module is loaded the
+// lookup and the attribute queries allocate nothing.
 struct DeviceSetup {
-  bool ready = false;
-  char *scratch = nullptr;  // device address of g_posv_scratch on this device
+  char *scratch = nullptr;  // device address of g_posv_scratch in the current context
   int sm_count = 0;
   int smem_optin = 0;
 };
 
-DeviceSetup g_setup[kMaxDevices];
-std::mutex g_setup_mutex;
-
-// Once per device, with that device current.
-int setup_device(int dev, DeviceSetup &out) {
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  DeviceSetup &s = g_setup[dev];
-  if (!s.ready) {
-    void *p = nullptr;
-    // g_posv_scratch names the array here only as a handle for the lookup;
-    // the host never dereferences it.
-    cudaError_t e = cudaGetSymbolAddress(&p, g_posv_scratch);
-    if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
-    int sms = 0, smem = 0;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return cuda_check(e, "cudaDeviceGetAttribute", __FILE__, __LINE__);
-    e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e != cudaSuccess) return cuda_check(e, "cudaDeviceGetAttribute", __FILE__, __LINE__);
-    s.scratch = static_cast<char *>(p);
-    s.sm_count = sms;
-    s.smem_optin = smem;
-    s.ready = true;
-  }
-  out = s;
+int setup_device(int dev, DeviceSetup &s) {
+  void *p = nullptr;
+  // g_posv_scratch names the array here only as a handle for the lookup; the
+  // host never dereferences it.
+  cudaError_t e = cudaGetSymbolAddress(&p, g_posv_scratch);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress", __FILE__, __LINE__);
+  e = cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaDeviceGetAttribute", __FILE__, __LINE__);
+  e = cudaDeviceGetAttribute(&s.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaDeviceGetAttribute", __FILE__, __LINE__);
+  s.scratch = static_cast<char *>(p);
   return KBLAS_Success;
 }
 
@@ -109,11 +99,6 @@ extern "C" int kblasDposv_batch_mixed_strided_noalloc(cudaStream_t stream, char 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice", __FILE__, __LINE__);
-  if (dev < 0 || dev >= kMaxDevices) {
-    fprintf(stderr, "kblasDposv_batch_mixed_strided_noalloc: device %d beyond the %d supported\n",
-            dev, kMaxDevices);
-    return KBLAS_NotSupported;
-  }
   DeviceSetup s;
   int st = setup_device(dev, s);
   if (st != KBLAS_Success) return st;
