@@ -244,15 +244,25 @@ def timed_steps(torch, fn, before, steps, warmup, stream):
 
 
 def measure_fp64_peak(kb, torch):
-    """Live FP64 FMA throughput (TFLOP/s) of this GPU: FMA chains, 16 warps/SM."""
+    """Live FP64 FMA throughput of this GPU (the denominator of every FP64-pipe
+    fraction): libkblas_probe.so's kblas_probe_fma (csrc/probe.cu) runs one
+    CTA per SM of 512 threads (16 warps), each thread ILP = 4 independent
+    chains of `iters` dependent FMAs; one warm-up launch and one launch timed
+    with CUDA events per repeat, best of 3 repeats. Returns the record."""
     p = kb.probe_lib()
     scratch = torch.zeros(1 << 20, dtype=torch.float64, device="cuda")
     nsm = torch.cuda.get_device_properties(0).multi_processor_count
-    best = 0.0
-    for _ in range(3):
-        ms = p.kblas_probe_fma(64, nsm, 512, 4096, 4, scratch.data_ptr())
-        best = max(best, 2.0 * nsm * 512 * 4096 * 4 / (ms * 1e-3) / 1e12)
-    return best
+    threads, iters, ilp, repeats = 512, 4096, 4, 3
+    times = []
+    for _ in range(repeats):
+        times.append(float(p.kblas_probe_fma(64, nsm, threads, iters, ilp, scratch.data_ptr())))
+    flop = 2.0 * nsm * threads * iters * ilp
+    best = max(flop / (ms * 1e-3) / 1e12 for ms in times)
+    return {"peak_tflops_measured_live": best,
+            "probe": {"kernel": "fma_chain_kernel<double, 4> (csrc/probe.cu)", "blocks": nsm,
+                      "threads_per_block": threads, "ilp_chains_per_thread": ilp,
+                      "fma_per_chain": iters, "flop_per_launch": flop, "repeats": repeats,
+                      "kernel_ms": [round(x, 4) for x in times], "statistic": "best of repeats"}}
 
 
 def accuracy_check(orc, w, torch, sample=1500, seed=0):
@@ -405,15 +415,6 @@ def _flops_potrf(n):
     return n ** 3 / 3.0 + n ** 2 / 2.0 + n / 6.0  # reference testing/flops.h POTRF
 
 
-def _line(metric, value, unit, ms, args, workload, extra):
-    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
-         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-         "config": {"workload": workload}}
-    d.update(extra)
-    print(json.dumps(d))
-
-
 def _dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
@@ -425,12 +426,362 @@ def _roof(fp64_peak, flops, bytes_, ms, peaks):
     return {"roofline": {"bound": "fp64 pipe (no FP64 tensor path on this part)",
                          "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": tf / fp64_peak, "traffic": None,
-                         "peak_source": "FP64 FMA chains measured live in this run"},
+                         "peak_source": "FP64 FMA chains measured live in this run (fp64_pipe)"},
             "hbm": {"achieved_gbs": gbs, "peak_gbs": hbm, "frac": gbs / hbm}}
 
 
+class Ctx:
+    """What the configuration runners share: the package, the oracle, one
+    handle on the current stream, the peaks."""
+
+    def __init__(self, args, torch, kb, wl, orc, h, stream, fp64_probe, peaks):
+        self.args, self.torch, self.kb, self.wl, self.orc = args, torch, kb, wl, orc
+        self.h, self.stream = h, stream
+        self.fp64 = fp64_probe
+        self.fp64_peak = fp64_probe["peak_tflops_measured_live"]
+        self.peaks = peaks
+        self.rng = np.random.default_rng(1)
+
+    def steps(self, k=None):
+        return k if k is not None else self.args.steps
+
+
+def _cpu_time(fn, make, seconds):
+    """Repeat fn(*make()) (inputs made outside the timer) for about `seconds`;
+    returns (calls, time)."""
+    spent, reps = 0.0, 0
+    while spent < seconds or reps == 0:
+        inp = make()
+        t0 = time.perf_counter()
+        fn(*inp)
+        spent += time.perf_counter() - t0
+        reps += 1
+    return reps, spent
+
+
+def cfg_potrf_potrs_n32(c, cpu_seconds=3.0):
+    """DPOTRF + DPOTRS, 10000 x n = 32, strided, one RHS. One timed step runs
+    REPS back-to-back POTRF + POTRS pairs, each on its own copy of the batch
+    (REPS x 82 MB, larger than L2), inside one CUDA event pair."""
+    torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
+    batch, n, reps = 10_000, 32, 100
+    a = wl.spd_shifted(batch, n, seed=0)
+    b = wl.rhs_rows(batch, 1, n, seed=0)
+    A0, B0 = _dev(torch, a), _dev(torch, b)
+    As = A0.unsqueeze(0).repeat(reps, 1, 1, 1)
+    Bs = B0.unsqueeze(0).repeat(reps, 1, 1, 1)
+    info = torch.zeros(reps, batch, dtype=torch.int32, device="cuda")
+    s2 = n * n
+
+    def step():
+        for r in range(reps):
+            kb.check(c.h.call("kblasDpotrf_batch_strided", "L", n, As[r].data_ptr(), n, s2, batch,
+                              info[r].data_ptr()), "potrf")
+            kb.check(c.h.call("kblasDpotrs_batch_strided", "R", "L", 1, n, As[r].data_ptr(), n,
+                              s2, Bs[r].data_ptr(), 1, n, batch), "potrs")
+
+    def restore():
+        As.copy_(A0.unsqueeze(0).expand_as(As))
+        Bs.copy_(B0.unsqueeze(0).expand_as(Bs))
+
+    with ClockSampler(0) as clk:
+        t = timed_steps(torch, step, restore, c.steps(), c.args.warmup, c.stream)
+    ms_step = float(np.mean(t))
+    ms = ms_step / reps  # one POTRF + POTRS pair over the batch
+    X = Bs[reps - 1].cpu().numpy()
+    pick = c.rng.choice(batch, 500, replace=False)
+    eta = orc.backward_error_r(a[pick], X[pick], b[pick], 1, n)
+    la = a[pick].copy()
+    info_ref = orc.potrf_batch(la, n)
+    L_ = As[reps - 1].cpu().numpy()
+    fac = max(orc.lower_rel_diff(L_[i], la[k], n) for k, i in enumerate(pick[:100]))
+    flops = batch * (_flops_potrf(n) + 2.0 * n * n)
+    bytes_ = batch * (8.0 * n * (n + 1) + 16.0 * n)
+    # CPU: the host LAPACK (dpotrf + dpotrs per matrix, OpenMP over the batch)
+    ca, cb = a[:2000].copy(), b[:2000].reshape(2000, 1, n).copy()
+    lp = orc.host_lapack()
+    if lp:
+        k, dt = _cpu_time(lambda x, y: orc.lapack_posv_batch(x, y), lambda: (ca.copy(), cb.copy()),
+                          cpu_seconds)
+        solver = lp[2]
+    else:
+        k, dt = _cpu_time(lambda x, y: orc.posv_batch(x, y, 1, n),
+                          lambda: (ca.copy(), b[:2000].copy()), cpu_seconds)
+        solver = "FP64 POTRF+POTRS, C restatement of LAPACK"
+    d = {"metric": "batched DPOTRF+DPOTRS solves/s (n=32)", "value": batch / (ms * 1e-3),
+         "unit": "solves/s", "ms_per_step": ms_step, "ms_per_call_pair": ms,
+         "fp64_gflops": flops / (ms * 1e-3) / 1e9,
+         "accuracy": {"checked": 500, "max_eta_over_10n_eps": float(eta.max() / (10 * n * EPS64)),
+                      "max_factor_rel_diff_vs_oracle": float(fac),
+                      "info_exact": bool(np.array_equal(info[reps - 1].cpu().numpy()[pick],
+                                                        info_ref))},
+         "gpu_launches": 2 * reps * c.steps(), "clocks": clk.summary(),
+         "cpu_baseline": {"value": 2000 * k / dt, "unit": "solves/s", "cores": os.cpu_count(),
+                          "kind": "port",
+                          "sample": f"2000 systems x {k} passes ({solver}, OpenMP over the batch)"},
+         "config": {"workload": "DPOTRF + DPOTRS, 10000 x n=32, strided, lda=32, 1 RHS, "
+                                "A = G G^T + 32 I",
+                    "timing": f"{reps} back-to-back POTRF+POTRS pairs per step, each on its own "
+                              f"copy of the batch ({reps * a.nbytes / 1e9:.1f} GB, larger than "
+                              f"L2), one CUDA event pair; value from the mean step"}}
+    d.update(_roof(c.fp64_peak, flops, bytes_, ms, c.peaks))
+    return d
+
+
+def cfg_trsm_trmm_syrk_n64(c, cpu_seconds=3.0):
+    torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
+    batch, n = 20_000, 64
+    L_ = wl.lower_tri(batch, n, seed=0, upper_fill=0.0)
+    Bm = wl.general(batch, n, n, seed=1)
+    Cs = wl.spd_shifted(batch, n, seed=2)
+    Am = wl.general(batch, n, n, seed=3)
+    dL, dB0, dC0, dA = _dev(torch, L_), _dev(torch, Bm), _dev(torch, Cs), _dev(torch, Am)
+    dB, dC = dB0.clone(), dC0.clone()
+    s2 = n * n
+    res = {}
+    pL = torch.from_numpy(dL.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+    pB = torch.from_numpy(dB.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+    pA = torch.from_numpy(dA.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+    pC = torch.from_numpy(dC.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
+    ops = {
+        "trsm_strided": lambda: h.call("kblasDtrsm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
+                                       dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch),
+        "trmm_strided": lambda: h.call("kblasDtrmm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
+                                       dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch),
+        "syrk_strided": lambda: h.call("kblasDsyrk_batch_strided", "L", "N", n, n, -1.0,
+                                       dA.data_ptr(), n, s2, 1.0, dC.data_ptr(), n, s2, batch),
+        "trsm_array": lambda: h.call("kblasDtrsm_batch", "L", "L", "N", "N", n, n, 1.0,
+                                     pL.data_ptr(), n, pB.data_ptr(), n, batch),
+        "trmm_array": lambda: h.call("kblasDtrmm_batch", "L", "L", "N", "N", n, n, 1.0,
+                                     pL.data_ptr(), n, pB.data_ptr(), n, batch),
+        "syrk_array": lambda: h.call("kblasDsyrk_batch", "L", "N", n, n, -1.0, pA.data_ptr(), n,
+                                     1.0, pC.data_ptr(), n, batch),
+    }
+    with ClockSampler(0) as clk:
+        for name, fn in ops.items():
+            def call(fn=fn, name=name):
+                kb.check(fn(), name)
+            restore = (lambda: dC.copy_(dC0)) if name.startswith("syrk") else (lambda: dB.copy_(dB0))
+            t = timed_steps(torch, call, restore, c.steps(), c.args.warmup, c.stream)
+            ms = float(np.mean(t))
+            if name.startswith("syrk"):
+                flops = batch * n * n * (n + 1.0)
+                bytes_ = batch * (8.0 * n * n + 16.0 * n * (n + 1) / 2)
+            else:
+                flops = batch * float(n) * n * n
+                bytes_ = batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n)
+            res[name] = {"ms": ms, "gflops": flops / (ms * 1e-3) / 1e9,
+                         "gbs": bytes_ / (ms * 1e-3) / 1e9,
+                         "fp64_frac": flops / (ms * 1e-3) / 1e12 / c.fp64_peak}
+    # accuracy on a sample against the oracle (strided forms)
+    pick = c.rng.choice(batch, 200, replace=False)
+    dB.copy_(dB0)
+    kb.check(ops["trsm_strided"](), "trsm")
+    X = dB.cpu().numpy()[pick]
+    ref = Bm[pick].copy()
+    orc.trsm_batch("L", "L", "N", "N", n, n, 1.0, L_[pick].copy(), ref)
+    trsm_err = float(np.abs(X - ref).max() / np.abs(ref).max())
+    dB.copy_(dB0)
+    kb.check(ops["trmm_strided"](), "trmm")
+    X = dB.cpu().numpy()[pick]
+    ref = Bm[pick].copy()
+    orc.trmm_batch("L", "L", "N", "N", n, n, 1.0, L_[pick].copy(), ref)
+    trmm_err = float(np.abs(X - ref).max() / np.abs(ref).max())
+    dC.copy_(dC0)
+    kb.check(ops["syrk_strided"](), "syrk")
+    Cg = dC.cpu().numpy()[pick]
+    Cr = Cs[pick].copy()
+    orc.syrk_batch("L", "N", n, n, -1.0, Am[pick].copy(), 1.0, Cr)
+    low = np.tril(np.ones((n, n), bool)).T  # column-major lower = upper of the stored array
+    syrk_err = float(np.abs((Cg - Cr)[:, low]).max() / np.abs(Cr[:, low]).max())
+    # CPU: the oracle's TRSM (C restatement of BLAS xTRSM), OpenMP over the batch
+    cl, cb = L_[:2000].copy(), Bm[:2000]
+    k, dt = _cpu_time(lambda x, y: orc.trsm_batch("L", "L", "N", "N", n, n, 1.0, x, y),
+                      lambda: (cl, cb.copy()), cpu_seconds)
+    ms = res["trsm_strided"]["ms"]
+    d = {"metric": "batched DTRSM GFLOP/s (64x64, strided; TRMM/SYRK in ops)",
+         "value": res["trsm_strided"]["gflops"], "unit": "GFLOP/s", "ms_per_step": ms,
+         "ops": res,
+         "accuracy": {"trsm_rel_err_vs_oracle": trsm_err, "trmm_rel_err_vs_oracle": trmm_err,
+                      "syrk_rel_err_vs_oracle": syrk_err},
+         "gpu_launches": 6 * c.steps(), "clocks": clk.summary(),
+         "cpu_baseline": {"value": 2000 * k * float(n) ** 3 / dt / 1e9, "unit": "GFLOP/s",
+                          "cores": os.cpu_count(), "kind": "port",
+                          "sample": f"DTRSM L,L,N,N 64x64, 2000 matrices x {k} passes (oracle's "
+                                    f"C restatement of BLAS xTRSM, OpenMP over the batch)"},
+         "config": {"workload": "DTRSM / DTRMM L,L,N,N 64x64 and DSYRK L,N 64x64, 20000 "
+                                "matrices, strided and pointer-array; value from the mean step"}}
+    d.update(_roof(c.fp64_peak, batch * float(n) ** 3,
+                   batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n), ms, c.peaks))
+    return d
+
+
+def cfg_posv_mixed(c, which, cpu_seconds=4.0):
+    """Mixed vs plain FP64 uniform DPOSV: the n = 64 conditioned batch with 4
+    RHS, or the n = 512 covariances with 8 RHS."""
+    torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
+    if which == "mixed_posv_n64":
+        batch, n, m = 50_000, 64, 4
+        a, cond = wl.spd_cond(batch, n, seed=0)
+        desc = ("mixed vs FP64 DPOSV, 50000 x n=64, cond log-uniform 1e2..1e8 (Q diag Q^T), "
+                "4 RHS, strided")
+    else:
+        batch, n, m = 2_000, 512, 8
+        a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range(batch // 100)])
+        desc = ("mixed vs FP64 DPOSV, 2000 x n=512 squared-exponential covariances, "
+                "l ~ U[0.05, 0.3], nugget 1e-4, 8 RHS, strided")
+    b = wl.rhs_rows(batch, m, n, seed=1)
+    A0, B0 = _dev(torch, a), _dev(torch, b)
+    A, B = A0.clone(), B0.clone()
+    info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    it = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    kb.lib().kblas_posv_batch_mixed_wsquery(h.ptr, b"R", m, n, batch)
+    kb.lib().kblas_posv_batch_strided_wsquery(h.ptr, b"R", m, n, batch)
+    kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
+
+    def restore():
+        A.copy_(A0)
+        B.copy_(B0)
+
+    def mixed():
+        kb.check(h.call("kblasDposv_batch_mixed_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
+                        B.data_ptr(), m, m * n, batch, info.data_ptr(), it.data_ptr()), "mixed")
+
+    def fp64():
+        kb.check(h.call("kblasDposv_batch_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
+                        B.data_ptr(), m, m * n, batch, info.data_ptr()), "posv")
+
+    with ClockSampler(0) as clk:
+        tm = timed_steps(torch, mixed, restore, c.steps(), c.args.warmup, c.stream)
+    Xm, itm, infom = B.cpu().numpy(), it.cpu().numpy(), info.cpu().numpy()
+    status = h.device_status()
+    tf = timed_steps(torch, fp64, restore, max(2, c.steps() // 2), 2, c.stream)
+    Xf, infof = B.cpu().numpy(), info.cpu().numpy()
+    ms_m, ms_f = float(np.mean(tm)), float(np.mean(tf))
+    ok = infof == 0
+    pick = np.where(ok)[0]
+    pick = pick[c.rng.choice(len(pick), min(len(pick), 400), replace=False)]
+    eta_m = orc.backward_error_r(a[pick], Xm[pick], b[pick], m, n)
+    eta_f = orc.backward_error_r(a[pick], Xf[pick], b[pick], m, n)
+    fwd = np.abs(Xm[pick] - Xf[pick]).max(axis=(1, 2)) / np.abs(Xf[pick]).max(axis=(1, 2))
+    ref_a, ref_b = a[pick].copy(), b[pick].copy()
+    info_o = orc.posv_batch(ref_a, ref_b, m, n)
+    den = np.abs(ref_b).max(axis=(1, 2))
+    fwd_om = np.abs(Xm[pick] - ref_b).max(axis=(1, 2)) / den
+    fwd_of = np.abs(Xf[pick] - ref_b).max(axis=(1, 2)) / den
+    flops = batch * (_flops_potrf(n) + 2.0 * m * n * n)
+    # CPU: host LAPACK dpotrf + dpotrs per system (B as n x m, LAPACK's layout)
+    ns = min(batch, 2000 if n <= 64 else 200)
+    ca = a[:ns].copy()
+    # b[k][i][r] = B(r, i); LAPACK solves A Y = B^T with Y n x m column-major:
+    # [k][r][i] = B(r, i)
+    cbt = np.ascontiguousarray(b[:ns].transpose(0, 2, 1))
+    lp = orc.host_lapack()
+    if lp:
+        k, dt = _cpu_time(lambda x, y: orc.lapack_posv_batch(x, y), lambda: (ca.copy(), cbt.copy()),
+                          cpu_seconds)
+        solver = lp[2]
+    else:
+        k, dt = _cpu_time(lambda x, y: orc.posv_batch(x, y, m, n), lambda: (ca.copy(), b[:ns].copy()),
+                          cpu_seconds)
+        solver = "FP64 POTRF+POTRS, C restatement of LAPACK"
+    d = {"metric": f"batched POSV solves/s (n={n}, {m} RHS): mixed-prec vs plain FP64",
+         "value": batch / (ms_m * 1e-3), "unit": "solves/s", "ms_per_step": ms_m,
+         "fp64_form": {"value": batch / (ms_f * 1e-3), "unit": "solves/s", "ms_per_step": ms_f,
+                       "max_eta_over_10n_eps": float(eta_f.max() / (10 * n * EPS64))},
+         "mixed_over_fp64": ms_f / ms_m,
+         "accuracy": {"checked": int(len(pick)),
+                      "max_eta_over_10n_eps": float(eta_m.max() / (10 * n * EPS64)),
+                      "all_within_bound": bool((eta_m <= 10 * n * EPS64).all()),
+                      "max_forward_rel_diff_vs_fp64": float(fwd.max()),
+                      "max_forward_rel_err_vs_oracle": float(fwd_om.max()),
+                      "fp64_form_max_forward_rel_err_vs_oracle": float(fwd_of.max()),
+                      "oracle_info_equal": bool(np.array_equal(info_o, infom[pick])),
+                      "info_equal_to_fp64_form": bool(np.array_equal(infom, infof))},
+         "refinement": {"mean_steps": float(itm[itm >= 0].mean()) if (itm >= 0).any() else None,
+                        "fallback_systems": int((itm < 0).sum()),
+                        "fallback_codes": {str(k_): int((itm == k_).sum()) for k_ in (-1, -2, -3, -4)
+                                           if (itm == k_).any()}},
+         "device_status": int(status),
+         "gpu_launches": c.steps(), "clocks": clk.summary(),
+         "cpu_baseline": {"value": ns * k / dt, "unit": "solves/s", "cores": os.cpu_count(),
+                          "kind": "port",
+                          "sample": f"{ns} systems x {k} passes ({solver}, OpenMP over the batch)"},
+         "config": {"workload": desc, "timing": "value from the mean step"}}
+    d.update(_roof(c.fp64_peak, flops, batch * (8.0 * n * (n + 1) + 16.0 * n * m), ms_f, c.peaks))
+    d["roofline"]["note"] = "roofline of the FP64 form (the mixed form uses FP32 + FP64)"
+    return d
+
+
+def cfg_inverse_n64(c):
+    torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
+    batch, n = 20_000, 64
+    a = wl.spd_shifted(batch, n, seed=0)
+    Lh = a.copy()
+    orc.potrf_batch(Lh, n)
+    A0, L0 = _dev(torch, a), _dev(torch, Lh)
+    W_ = A0.clone()
+    info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+    fl = {"trtri": n ** 3 / 3.0, "lauum": n ** 3 / 3.0, "potri": 2 * n ** 3 / 3.0, "poti": n ** 3}
+    res = {}
+    for op in ("trtri", "lauum", "potri", "poti"):
+        src = A0 if op == "poti" else L0
+        flags = ("L", "N") if op == "trtri" else ("L",)
+
+        def fn(op=op, flags=flags):
+            kb.check(h.call(f"kblasD{op}_batch_strided", *flags, n, W_.data_ptr(), n, n * n,
+                            batch, info.data_ptr()), op)
+        t = timed_steps(torch, fn, lambda src=src: W_.copy_(src), c.steps(), c.args.warmup,
+                        c.stream)
+        ms = float(np.mean(t))
+        res[op] = {"ms": ms, "gflops": batch * fl[op] / (ms * 1e-3) / 1e9,
+                   "fp64_frac": batch * fl[op] / (ms * 1e-3) / 1e12 / c.fp64_peak}
+    pick = c.rng.choice(batch, 200, replace=False)
+    W_.copy_(A0)
+    kb.check(h.call("kblasDpoti_batch_strided", "L", n, W_.data_ptr(), n, n * n, batch,
+                    info.data_ptr()), "poti")
+    got = W_.cpu().numpy()[pick]
+    ref = a[pick].copy()
+    orc.poti_batch(ref, n)
+    low = np.triu(np.ones((n, n), bool))
+    err = float(np.abs((got - ref)[:, low]).max() / np.abs(ref[:, low]).max())
+    cs = a[:2000]
+    k, dt = _cpu_time(lambda x: orc.poti_batch(x, n), lambda: (cs.copy(),), 3.0)
+    ms = res["poti"]["ms"]
+    d = {"metric": "batched DPOTI inverses/s (n=64; TRTRI/LAUUM/POTRI in ops)",
+         "value": batch / (ms * 1e-3), "unit": "inverses/s", "ms_per_step": ms, "ops": res,
+         "accuracy": {"poti_rel_err_vs_oracle": err},
+         "gpu_launches": c.steps(),
+         "cpu_baseline": {"value": 2000 * k / dt, "unit": "inverses/s", "cores": os.cpu_count(),
+                          "kind": "port", "sample": f"POTI, 2000 matrices x {k} passes"},
+         "config": {"workload": "DTRTRI / DLAUUM / DPOTRI / DPOTI, 20000 x n=64, strided, "
+                                "lower, A = G G^T + 64 I"}}
+    d.update(_roof(c.fp64_peak, batch * fl["poti"], batch * 16.0 * n * (n + 1) / 2, ms, c.peaks))
+    return d
+
+
+def make_ctx(args, torch, kb, wl, orc, h, stream):
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    return Ctx(args, torch, kb, wl, orc, h, stream, measure_fp64_peak(kb, torch), peaks)
+
+
+CONFIGS = {
+    "potrf_potrs_n32": cfg_potrf_potrs_n32,
+    "trsm_trmm_syrk_n64": cfg_trsm_trmm_syrk_n64,
+    "mixed_posv_n64": lambda c: cfg_posv_mixed(c, "mixed_posv_n64"),
+    "posv_n512": lambda c: cfg_posv_mixed(c, "posv_n512"),
+    "inverse_n64": cfg_inverse_n64,
+    "gemm_vbatch": lambda c: run_gemm_vbatch(c),
+}
+
+
 def run_workload(args):
-    """The configurations besides the variable-size headline."""
+    """One configuration besides the variable-size headline, as its own JSON
+    line."""
     import torch
     torch.cuda.set_device(0)
     kb, wl = load_pkg()
@@ -438,277 +789,23 @@ def run_workload(args):
     orc.build()
     stream = torch.cuda.current_stream()
     h = kb.Handle(stream=stream.cuda_stream)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    fp64_peak = measure_fp64_peak(kb, torch)
-    rng = np.random.default_rng(1)
-    W = args.workload
-
-    if W == "potrf_potrs_n32":
-        batch, n = 10_000, 32
-        a = wl.spd_shifted(batch, n, seed=0)
-        b = wl.rhs_rows(batch, 1, n, seed=0)
-        A0, B0 = _dev(torch, a), _dev(torch, b)
-        A, B = A0.clone(), B0.clone()
-        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
-
-        def step():
-            kb.check(h.call("kblasDpotrf_batch_strided", "L", n, A.data_ptr(), n, n * n, batch,
-                            info.data_ptr()), "potrf")
-            kb.check(h.call("kblasDpotrs_batch_strided", "R", "L", 1, n, A.data_ptr(), n, n * n,
-                            B.data_ptr(), 1, n, batch), "potrs")
-
-        def restore():
-            A.copy_(A0)
-            B.copy_(B0)
-
-        with ClockSampler(0) as clk:
-            t = timed_steps(torch, step, restore, args.steps, args.warmup, stream)
-        ms = float(np.median(t))
-        X = B.cpu().numpy()
-        pick = rng.choice(batch, 500, replace=False)
-        eta = orc.backward_error_r(a[pick], X[pick], b[pick], 1, n)
-        la = a[pick].copy()
-        info_ref = orc.potrf_batch(la, n)
-        flops = batch * (_flops_potrf(n) + 2.0 * n * n)
-        bytes_ = batch * (8.0 * n * (n + 1) + 16.0 * n)
-        cs = a[:2000].copy(); cb = b[:2000].copy()
-        lp = orc.host_lapack()
-        solver = lp[2] if lp else "FP64 POTRF+POTRS, C restatement of LAPACK"
-        spent, reps = 0.0, 0
-        while spent < 3.0:
-            x1, y1 = cs.copy(), cb.copy()  # fresh copies, outside the timer
-            t0 = time.perf_counter()
-            if lp:
-                orc.lapack_posv1_vbatch([n] * 2000, list(x1), [n] * 2000, list(y1))
-            else:
-                orc.posv_batch(x1, y1, 1, n)
-            spent += time.perf_counter() - t0
-            reps += 1
-        cpu = 2000 * reps / spent
-        ex = {"fp64_gflops": flops / (ms * 1e-3) / 1e9,
-              "accuracy": {"checked": 500, "max_eta_over_10n_eps": float(eta.max() / (10 * n * EPS64)),
-                           "info_exact": bool(np.array_equal(info.cpu().numpy()[pick], info_ref))},
-              "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
-              "cpu_baseline": {"value": cpu, "unit": "solves/s", "cores": os.cpu_count(),
-                               "kind": "port",
-                               "sample": f"2000 systems x {reps} passes ({solver}, OpenMP over the batch)"}}
-        ex.update(_roof(fp64_peak, flops, bytes_, ms, peaks))
-        ex["config"] = {"workload": "DPOTRF + DPOTRS, 10000 x n=32, strided, lda=32, 1 RHS, "
-                                    "A = G G^T + 32 I"}
-        _line("batched DPOTRF+DPOTRS solves/s (n=32)", batch / (ms * 1e-3), "solves/s", ms, args,
-              "", ex)
-        return 0
-
-    if W == "trsm_trmm_syrk_n64":
-        batch, n = 20_000, 64
-        L_ = wl.lower_tri(batch, n, seed=0, upper_fill=0.0)
-        Bm = wl.general(batch, n, n, seed=1)
-        Cs = wl.spd_shifted(batch, n, seed=2)
-        Am = wl.general(batch, n, n, seed=3)
-        dL, dB0, dC0, dA = _dev(torch, L_), _dev(torch, Bm), _dev(torch, Cs), _dev(torch, Am)
-        dB, dC = dB0.clone(), dC0.clone()
-        s2 = n * n
-        res = {}
-        for form in ("strided", "array"):
-            pL = torch.from_numpy(dL.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
-            pB = torch.from_numpy(dB.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
-            pA = torch.from_numpy(dA.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
-            pC = torch.from_numpy(dC.data_ptr() + np.arange(batch, dtype=np.int64) * s2 * 8).cuda()
-            ops = {}
-            if form == "strided":
-                ops["trsm"] = lambda: h.call("kblasDtrsm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
-                                             dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch)
-                ops["trmm"] = lambda: h.call("kblasDtrmm_batch_strided", "L", "L", "N", "N", n, n, 1.0,
-                                             dL.data_ptr(), n, s2, dB.data_ptr(), n, s2, batch)
-                ops["syrk"] = lambda: h.call("kblasDsyrk_batch_strided", "L", "N", n, n, -1.0,
-                                             dA.data_ptr(), n, s2, 1.0, dC.data_ptr(), n, s2, batch)
-            else:
-                ops["trsm"] = lambda: h.call("kblasDtrsm_batch", "L", "L", "N", "N", n, n, 1.0,
-                                             pL.data_ptr(), n, pB.data_ptr(), n, batch)
-                ops["trmm"] = lambda: h.call("kblasDtrmm_batch", "L", "L", "N", "N", n, n, 1.0,
-                                             pL.data_ptr(), n, pB.data_ptr(), n, batch)
-                ops["syrk"] = lambda: h.call("kblasDsyrk_batch", "L", "N", n, n, -1.0,
-                                             pA.data_ptr(), n, 1.0, pC.data_ptr(), n, batch)
-            for name, fn in ops.items():
-                def call(fn=fn, name=name):
-                    kb.check(fn(), name)
-                restore = (lambda: dC.copy_(dC0)) if name == "syrk" else (lambda: dB.copy_(dB0))
-                t = timed_steps(torch, call, restore, args.steps, args.warmup, stream)
-                ms = float(np.median(t))
-                if name == "syrk":
-                    flops = batch * n * n * (n + 1.0)
-                    bytes_ = batch * (8.0 * n * n + 16.0 * n * (n + 1) / 2)
-                else:
-                    flops = batch * float(n) * n * n
-                    bytes_ = batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n)
-                res[f"{name}_{form}"] = {"ms": ms, "gflops": flops / (ms * 1e-3) / 1e9,
-                                         "gbs": bytes_ / (ms * 1e-3) / 1e9,
-                                         "fp64_frac": flops / (ms * 1e-3) / 1e12 / fp64_peak}
-        # accuracy on a sample (strided results of the last runs)
-        pick = rng.choice(batch, 200, replace=False)
-        dB.copy_(dB0)
-        kb.check(h.call("kblasDtrsm_batch_strided", "L", "L", "N", "N", n, n, 1.0, dL.data_ptr(), n,
-                        s2, dB.data_ptr(), n, s2, batch), "trsm")
-        X = dB.cpu().numpy()[pick]
-        ref = Bm[pick].copy()
-        orc.trsm_batch("L", "L", "N", "N", n, n, 1.0, L_[pick].copy(), ref)
-        trsm_err = float(np.abs(X - ref).max() / np.abs(ref).max())
-        dC.copy_(dC0)
-        kb.check(h.call("kblasDsyrk_batch_strided", "L", "N", n, n, -1.0, dA.data_ptr(), n, s2, 1.0,
-                        dC.data_ptr(), n, s2, batch), "syrk")
-        Cg = dC.cpu().numpy()[pick]
-        Cr = Cs[pick].copy()
-        orc.syrk_batch("L", "N", n, n, -1.0, Am[pick].copy(), 1.0, Cr)
-        low = np.tril(np.ones((n, n), bool)).T  # column-major lower = upper of the stored array
-        syrk_err = float(np.abs((Cg - Cr)[:, low]).max() / np.abs(Cr[:, low]).max())
-        ms = res["trsm_strided"]["ms"]
-        ex = {"ops": res, "accuracy": {"trsm_rel_err": trsm_err, "syrk_rel_err": syrk_err},
-              "gpu_launches": 6 * args.steps,
-              "config": {"workload": "DTRSM / DTRMM L,L,N,N 64x64 and DSYRK L,N 64x64, 20000 "
-                                     "matrices, strided and pointer-array"}}
-        ex.update(_roof(fp64_peak, batch * float(n) ** 3, batch * (8.0 * n * (n + 1) / 2 + 16.0 * n * n),
-                        ms, peaks))
-        _line("batched DTRSM GFLOP/s (64x64, strided; TRMM/SYRK in ops)",
-              res["trsm_strided"]["gflops"], "GFLOP/s", ms, args, "", ex)
-        return 0
-
-    if W in ("mixed_posv_n64", "posv_n512"):
-        if W == "mixed_posv_n64":
-            batch, n, m = 50_000, 64, 4
-            a, cond = wl.spd_cond(batch, n, seed=0)
-            desc = ("mixed vs FP64 DPOSV, 50000 x n=64, cond log-uniform 1e2..1e8 (Q diag Q^T), "
-                    "4 RHS, strided")
-        else:
-            batch, n, m = 2_000, 512, 8
-            a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range(batch // 100)])
-            cond = None
-            desc = ("mixed vs FP64 DPOSV, 2000 x n=512 squared-exponential covariances, "
-                    "l ~ U[0.05, 0.3], nugget 1e-4, 8 RHS, strided")
-        b = wl.rhs_rows(batch, m, n, seed=1)
-        A0, B0 = _dev(torch, a), _dev(torch, b)
-        A, B = A0.clone(), B0.clone()
-        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
-        it = torch.zeros(batch, dtype=torch.int32, device="cuda")
-        kb.lib().kblas_posv_batch_mixed_wsquery(h.ptr, b"R", m, n, batch)
-        kb.lib().kblas_posv_batch_strided_wsquery(h.ptr, b"R", m, n, batch)
-        kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
-
-        def restore():
-            A.copy_(A0)
-            B.copy_(B0)
-
-        def mixed():
-            kb.check(h.call("kblasDposv_batch_mixed_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
-                            B.data_ptr(), m, m * n, batch, info.data_ptr(), it.data_ptr()), "mixed")
-
-        def fp64():
-            kb.check(h.call("kblasDposv_batch_strided", "R", "L", m, n, A.data_ptr(), n, n * n,
-                            B.data_ptr(), m, m * n, batch, info.data_ptr()), "posv")
-
-        with ClockSampler(0) as clk:
-            tm = timed_steps(torch, mixed, restore, args.steps, args.warmup, stream)
-        Xm, itm, infom = B.cpu().numpy(), it.cpu().numpy(), info.cpu().numpy()
-        tf = timed_steps(torch, fp64, restore, max(2, args.steps // 2), 2, stream)
-        Xf, infof = B.cpu().numpy(), info.cpu().numpy()
-        ms_m, ms_f = float(np.median(tm)), float(np.median(tf))
-        ok = infof == 0
-        pick = np.where(ok)[0]
-        pick = pick[rng.choice(len(pick), min(len(pick), 400), replace=False)]
-        eta_m = orc.backward_error_r(a[pick], Xm[pick], b[pick], m, n)
-        eta_f = orc.backward_error_r(a[pick], Xf[pick], b[pick], m, n)
-        fwd = np.abs(Xm[pick] - Xf[pick]).max(axis=(1, 2)) / np.abs(Xf[pick]).max(axis=(1, 2))
-        # forward errors of both forms against the oracle's FP64 LAPACK-style solution
-        ref_a, ref_b = a[pick].copy(), b[pick].copy()
-        info_o = orc.posv_batch(ref_a, ref_b, m, n)
-        den = np.abs(ref_b).max(axis=(1, 2))
-        fwd_om = np.abs(Xm[pick] - ref_b).max(axis=(1, 2)) / den
-        fwd_of = np.abs(Xf[pick] - ref_b).max(axis=(1, 2)) / den
-        flops = batch * (_flops_potrf(n) + 2.0 * m * n * n)
-        ex = {"fp64_form": {"value": batch / (ms_f * 1e-3), "unit": "solves/s", "ms_per_step": ms_f,
-                            "max_eta_over_10n_eps": float(eta_f.max() / (10 * n * EPS64))},
-              "mixed_over_fp64": ms_f / ms_m,
-              "accuracy": {"checked": int(len(pick)),
-                           "max_eta_over_10n_eps": float(eta_m.max() / (10 * n * EPS64)),
-                           "all_within_bound": bool((eta_m <= 10 * n * EPS64).all()),
-                           "max_forward_rel_diff_vs_fp64": float(fwd.max()),
-                           "max_forward_rel_err_vs_oracle": float(fwd_om.max()),
-                           "fp64_form_max_forward_rel_err_vs_oracle": float(fwd_of.max()),
-                           "oracle_info_equal": bool(np.array_equal(info_o, infom[pick])),
-                           "info_equal_to_fp64_form": bool(np.array_equal(infom, infof))},
-              "refinement": {"mean_steps": float(itm[itm >= 0].mean()) if (itm >= 0).any() else None,
-                             "fallback_systems": int((itm < 0).sum())},
-              "gpu_launches": args.steps, "clocks": clk.summary(),
-              "config": {"workload": desc}}
-        ex.update(_roof(fp64_peak, flops, batch * (8.0 * n * (n + 1) + 16.0 * n * m), ms_f, peaks))
-        ex["roofline"]["note"] = "roofline of the FP64 form (the mixed form uses FP32 + FP64)"
-        _line(f"batched POSV solves/s (n={n}, {m} RHS): mixed-prec vs plain FP64",
-              batch / (ms_m * 1e-3), "solves/s", ms_m, args, "", ex)
-        return 0
-    if W == "inverse_n64":
-        batch, n = 20_000, 64
-        a = wl.spd_shifted(batch, n, seed=0)
-        Lh = a.copy()
-        orc.potrf_batch(Lh, n)
-        A0, L0 = _dev(torch, a), _dev(torch, Lh)
-        W_ = A0.clone()
-        info = torch.zeros(batch, dtype=torch.int32, device="cuda")
-        fl = {"trtri": n ** 3 / 3.0, "lauum": n ** 3 / 3.0, "potri": 2 * n ** 3 / 3.0,
-              "poti": n ** 3}
-        res = {}
-        for op in ("trtri", "lauum", "potri", "poti"):
-            src = A0 if op == "poti" else L0
-            flags = ("L", "N") if op == "trtri" else ("L",)
-
-            def fn(op=op, flags=flags):
-                kb.check(h.call(f"kblasD{op}_batch_strided", *flags, n, W_.data_ptr(), n, n * n,
-                                batch, info.data_ptr()), op)
-            t = timed_steps(torch, fn, lambda src=src: W_.copy_(src), args.steps, args.warmup,
-                            stream)
-            ms = float(np.median(t))
-            res[op] = {"ms": ms, "gflops": batch * fl[op] / (ms * 1e-3) / 1e9,
-                       "fp64_frac": batch * fl[op] / (ms * 1e-3) / 1e12 / fp64_peak}
-        # accuracy of POTI on a sample against the oracle, CPU baseline of POTI
-        pick = rng.choice(batch, 200, replace=False)
-        W_.copy_(A0)
-        kb.check(h.call("kblasDpoti_batch_strided", "L", n, W_.data_ptr(), n, n * n, batch,
-                        info.data_ptr()), "poti")
-        got = W_.cpu().numpy()[pick]
-        ref = a[pick].copy()
-        orc.poti_batch(ref, n)
-        low = np.triu(np.ones((n, n), bool))
-        err = float(np.abs((got - ref)[:, low]).max() / np.abs(ref[:, low]).max())
-        cs = a[:2000].copy()
-        t0 = time.perf_counter()
-        reps = 0
-        while time.perf_counter() - t0 < 3.0:
-            x1 = cs.copy()
-            orc.poti_batch(x1, n)
-            reps += 1
-        cpu = 2000 * reps / (time.perf_counter() - t0)
-        ms = res["poti"]["ms"]
-        ex = {"ops": res, "accuracy": {"poti_rel_err_vs_oracle": err},
-              "gpu_launches": args.steps,
-              "cpu_baseline": {"value": cpu, "unit": "inverses/s", "cores": os.cpu_count(),
-                               "kind": "port", "sample": f"POTI, 2000 matrices x {reps} passes"},
-              "config": {"workload": "DTRTRI / DLAUUM / DPOTRI / DPOTI, 20000 x n=64, strided, "
-                                     "lower, A = G G^T + 64 I"}}
-        ex.update(_roof(fp64_peak, batch * fl["poti"], batch * 16.0 * n * (n + 1) / 2, ms, peaks))
-        _line("batched DPOTI inverses/s (n=64; TRTRI/LAUUM/POTRI in ops)", batch / (ms * 1e-3),
-              "inverses/s", ms, args, "", ex)
-        return 0
-    if W == "gemm_vbatch":
-        return run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng)
-    raise SystemExit(f"unknown workload {W}")
+    c = make_ctx(args, torch, kb, wl, orc, h, stream)
+    d = CONFIGS[args.workload](c)
+    line = {"metric": d.pop("metric"), "value": d.pop("value"), "unit": d.pop("unit"), "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": d.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "fp64_pipe": c.fp64}
+    line.update(d)
+    print(json.dumps(line))
+    return 0
 
 
-def run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng):
+def run_gemm_vbatch(c):
     """Batched DGEMM (uniform 64^3, beside cuBLAS through torch.bmm, which is
     what the reference's uniform GEMM calls) and the variable-size DGEMM /
     DSYRK / DTRSM, sizes uniform in 16..128, pointer arrays."""
+    args, torch, kb, wl, orc, h, stream = c.args, c.torch, c.kb, c.wl, c.orc, c.h, c.stream
+    fp64_peak, peaks, rng = c.fp64_peak, c.peaks, c.rng
     res = {}
     # uniform: 20000 x 64x64x64, C := A B + C (--batch below 20000 shrinks both
     # parts, for profiler captures)
@@ -730,7 +827,7 @@ def run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng):
     flops_u = 2.0 * batch * n ** 3
     for name, fn in (("dgemm_uniform_64", ours), ("cublas_bmm_uniform_64", cublas)):
         t = timed_steps(torch, fn, lambda: C.copy_(C0), args.steps, args.warmup, stream)
-        ms = float(np.median(t))
+        ms = float(np.mean(t))
         res[name] = {"ms": ms, "gflops": flops_u / (ms * 1e-3) / 1e9,
                      "fp64_frac": flops_u / (ms * 1e-3) / 1e12 / fp64_peak}
     C.copy_(C0)
@@ -797,7 +894,7 @@ def run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng):
                               ("dsyrk_vbatch", vsyrk, lambda: Sb.copy_(Sb0)),
                               ("dtrsm_vbatch", vtrsm, lambda: Xb.copy_(Xb0))):
             t = timed_steps(torch, fn, rst, args.steps, args.warmup, stream)
-            ms = float(np.median(t))
+            ms = float(np.mean(t))
             res[name] = {"ms": ms, "gflops": fl[name] / (ms * 1e-3) / 1e9,
                          "fp64_frac": fl[name] / (ms * 1e-3) / 1e12 / fp64_peak}
     # accuracy of the variable-size GEMM on a sample against the oracle
@@ -839,9 +936,9 @@ def run_gemm_vbatch(args, torch, kb, wl, orc, h, stream, fp64_peak, peaks, rng):
                                  f"pointer arrays, sizes in device arrays"}}
     bytes_ = 8.0 * float((ms_.astype(np.float64) * ks_ + ks_ * ns_ + 2.0 * ms_ * ns_).sum())
     ex.update(_roof(fp64_peak, fl["dgemm_vbatch"], bytes_, ms, peaks))
-    _line("variable-size batched DGEMM GFLOP/s (m, n, k in 16..128)", res["dgemm_vbatch"]["gflops"],
-          "GFLOP/s", ms, args, "", ex)
-    return 0
+    ex.update({"metric": "variable-size batched DGEMM GFLOP/s (m, n, k in 16..128)",
+               "value": res["dgemm_vbatch"]["gflops"], "unit": "GFLOP/s", "ms_per_step": ms})
+    return ex
 
 
 def main():
@@ -852,6 +949,8 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--batch", type=int, default=100_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the other configurations after the variable-size headline")
     ap.add_argument("--workload", default="vbatch",
                     choices=["vbatch", "potrf_potrs_n32", "trsm_trmm_syrk_n64", "mixed_posv_n64",
                              "posv_n512", "inverse_n64", "gemm_vbatch"])
@@ -999,7 +1098,8 @@ def main():
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     ab = w.alg_bytes()
     achieved = ab / (ms_mixed * 1e-3) / 1e9
-    fp64_peak = measure_fp64_peak(kb, torch)
+    fp64_rec = measure_fp64_peak(kb, torch)
+    fp64_peak = fp64_rec["peak_tflops_measured_live"]
     steps_arr = it[(info == 0) & (it >= 0)]
     fp64_flops_refine = float((2.0 * w.ns.astype(np.float64) ** 2 *
                                np.where(it >= 0, it + 1, 0)).sum())
@@ -1031,7 +1131,7 @@ def main():
                              "trips); ncu: DRAM throughput 1.6%, FP64 pipe 23%, FP32 8% "
                              "(profiles/posv_vbatch_mixed_n8-256.txt). The FP64 form's "
                              "fraction of the FP64 pipe is in fp64_pipe"},
-        "fp64_pipe": {"peak_tflops_measured_live": fp64_peak,
+        "fp64_pipe": {"peak_tflops_measured_live": fp64_peak, "probe": fp64_rec["probe"],
                       "refinement_fp64_tflops": fp64_flops_refine / (ms_mixed * 1e-3) / 1e12,
                       "fp64_form_tflops": useful / (ms_fp64 * 1e-3) / 1e12,
                       "fp64_form_frac": useful / (ms_fp64 * 1e-3) / 1e12 / fp64_peak},
@@ -1051,8 +1151,23 @@ def main():
         "gpu_launches": 5 * args.steps,
         "clocks": clk.summary(),
     }
+    line["device_status"] = h.device_status()
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(orc, wl)
+    if rank == 0 and not args.headline_only:
+        # the other configurations of the path, each with its own value,
+        # accuracy against the oracle, roofline and CPU baseline
+        del w
+        torch.cuda.empty_cache()
+        c = make_ctx(args, torch, kb, wl, orc, h, stream)
+        c.fp64 = fp64_rec
+        c.fp64_peak = fp64_peak
+        line["configs"] = {}
+        for name in ("potrf_potrs_n32", "trsm_trmm_syrk_n64", "mixed_posv_n64", "posv_n512"):
+            t0 = time.perf_counter()
+            line["configs"][name] = CONFIGS[name](c)
+            line["configs"][name]["wall_s"] = round(time.perf_counter() - t0, 1)
+            torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line))
     h.close()

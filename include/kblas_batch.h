@@ -439,7 +439,8 @@ int kblasZtrsm_vbatch(kblasHandle_t handle, char side, char uplo, char trans, ch
  * >= 0 refinement steps taken (A is unchanged); < 0 the FP64 path was used
  * (A holds L): -1 FP32 pivot test failed, -2 refinement stalled (error not
  * halved by a step, or contracting too slowly for the remaining steps to cost
- * less than the FP64 factorization), -3 step cap.
+ * less than the FP64 factorization), -3 step cap, -4 routed to the FP64 path
+ * before any refinement by the conditioning estimate of kblasSetPosvRouting.
  * info_array as for POSV. Needs workspace: kblas_posv_batch_mixed_wsquery. */
 void kblas_posv_batch_mixed_wsquery(kblasHandle_t handle, char side, const int m, const int n,
                                     int batchCount);
@@ -480,6 +481,14 @@ int kblasDposv_vbatch_mixed(kblasHandle_t handle, char side, char uplo,
 #define KBLAS_POSV_TUNING_CLASSES 8
 int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi);
 
+/* Routing constant of the mixed-precision POSV: after the FP32
+ * factorization, a system whose predicted refinement (contraction estimated
+ * as c * 2^-24 / d_min, d_min the smallest pivot of the scaled factor) would
+ * cost more FP64 work than the FP64 factorization goes straight to the FP64
+ * path (iter = -4). c > 0 sets the constant, c == 0 turns the routing off,
+ * c < 0 restores the compiled one. Used by the committed autotuner. */
+int kblasSetPosvRouting(double c);
+
 /* Allocation-free mixed-precision POSV (no counterpart in the reference).
  * Same arguments, semantics and results as kblasDposv_batch_mixed_strided,
  * but it takes a CUDA stream instead of a handle and allocates nothing: its
@@ -504,9 +513,11 @@ int kblasDposv_batch_mixed_strided_noalloc(cudaStream_t stream, char side, char 
                                            double *B, int ldb, long strideB,
                                            int batchCount, int *info_array, int *iter_array);
 
-/* Status word of the last persistent launch on this handle (read by the host
- * after the stream completes): KBLAS_Success, or KBLAS_Error_Timeout if a
- * bounded device-side wait ran out. Synchronises the handle's stream. */
+/* Device status word of the handle's mixed-precision launches (no reference
+ * counterpart): KBLAS_Success, or KBLAS_Error_Timeout if, in any launch since
+ * the last read, a bounded device-side wait for the tensor-core MMAs ran out
+ * (that launch stopped without writing its results). Synchronises the handle's
+ * stream and clears the word. */
 int kblasGetDeviceStatus(kblasHandle_t handle);
 
 #ifdef __cplusplus

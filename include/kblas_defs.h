@@ -36,8 +36,10 @@
 #define KBLAS_MAGMA_Error           -11
 #define KBLAS_SVD_NoConvergence     -12
 
-/* Status code added by this library: a persistent kernel's bounded wait ran out
- * (a work item was never published). No reference counterpart. */
+/* Status code added by this library: a bounded device-side wait of the
+ * mixed-precision persistent kernel (for its tensor-core MMAs) ran out; the
+ * kernel stopped without writing results. Reported by kblasGetDeviceStatus.
+ * No reference counterpart. */
 #define KBLAS_Error_Timeout         -13
 
 #define KBLAS_NSTREAMS 10

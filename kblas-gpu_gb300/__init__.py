@@ -90,6 +90,7 @@ _SIG = {
     "kblasDposv_vbatch": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P]),
     "kblasDposv_vbatch_mixed": (I, [P, CH, CH, P, P, I, I, P, P, P, P, I, P, P]),
     "kblasSetPosvTuning": (I, [I, P, P, P]),
+    "kblasSetPosvRouting": (I, [D]),
     "kblas_trtri_batch_wsquery": (None, [P, I, I]),
     "kblas_trtri_batch_strided_wsquery": (None, [P, I, I]),
     "kblas_lauum_batch_wsquery": (None, [P, I, I]),

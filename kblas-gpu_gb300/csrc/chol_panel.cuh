@@ -19,6 +19,7 @@
 #pragma once
 
 #include "device_util.cuh"
+#include "tc_util.cuh"
 #include "team.cuh"
 
 namespace kgb {
@@ -370,6 +371,233 @@ __device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T 
   __syncwarp();
 }
 
+// The trailing update of step p by warps 1.. of a look-ahead team, FP32/FP64
+// FMAs in 4 x 4 register tiles; the next panel's diagonal block (warp 0's)
+// is skipped.
+template <typename T>
+__device__ __forceinline__ void trailing_update_ffma(const Team &t, const PanelLayout &L, int p, T *Ps)
+{
+  const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+  const T *Pp = Ps + L.base(p);
+  const int utid = t.tid - 32, unt = t.nt - 32;
+  int tile0 = 0;
+  for (int q = p + 1; q < L.np; q++) {
+    const int K = q * PNB, mq = L.n - K, jq = L.jb(q);
+    const int rt = (mq + 3) >> 2, ct = (jq + 3) >> 2;
+    const int ntile = rt * ct;
+    T *Pq = Ps + L.base(q);
+    const int ldq = L.ldp(q);
+    const int start = ((utid - tile0) % unt + unt) % unt;
+    for (int tt = start; tt < ntile; tt += unt) {
+      const int c4 = tt / rt, r4 = tt - c4 * rt;
+      if (q == p + 1 && r4 < 8) continue;  // the next diagonal block: warp 0
+      if (r4 * 4 + 3 < c4 * 4) continue;
+      panel_tile_update<T>(Pp, ld, jb, K - J, r4 * 4, c4 * 4, Pq, ldq, jq);
+    }
+    tile0 += ntile;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Tensor-core trailing update (FP32 factor; a team that is the whole CTA).
+//
+// Step p's update of the trailing lower triangle, C -= P P^T with P the R =
+// n - 32 (p + 1) rows of panel p below its diagonal block (K = 32), runs as
+// BF16 products on the tensor cores with FP32 accumulation in TMEM. Each P
+// entry is split into three BF16 terms, x = hi + mid + lo (to 2^-24 |x|), and
+// the six products whose order is at most 2^-16 -- hi hi, hi mid, mid hi,
+// hi lo, lo hi, mid mid -- are accumulated (the dropped terms are of order
+// 2^-24 |x||y|): the hi + lo split of two BF16 terms extended by one term, so
+// that the update stays close to FP32 accuracy and the refinement converges as
+// with an FP32 FMA update (with two terms the factor would carry ~2^-16
+// relative errors and need more FP64 refinement sweeps).
+//
+// Work split: warp 0 keeps its look-ahead (it updates and factors the next
+// diagonal block with FP32 FMAs); warps 1.. stage P as the three BF16 terms
+// in the no-swizzle K-major layout of tc_util.cuh, one of them issues the
+// MMAs (M = 128 row tiles of the trailing matrix, N up to 256 columns per
+// instruction, 2 x 6 instructions per tile and column chunk), and after the
+// mbarrier reports completion every warp subtracts its TMEM lanes' results
+// from the panel storage (lane = row: conflict-free column accesses).
+// Row tiles start at multiples of 128; the last one starts at
+// round_up8(R - 128) so that it ends at or past R (staged rows beyond R are
+// zero and their results are dropped); tiles own disjoint row ranges. TMEM
+// (512 columns) is filled with as many (tile, column chunk) pairs per round as
+// fit; large orders take several rounds.
+struct TcCtx {
+  uint32_t tmem;         // TMEM address (lane 0, column 0) of the CTA's columns
+  uint64_t *bar;         // MMA completion mbarrier (one arrival per round)
+  unsigned char *stage;  // 3 x rows_pad x 64 bytes of shared memory, 16-byte aligned
+  int *abort;            // shared flag: a bounded wait ran out
+  int *status;           // device status word of the launch (may be null)
+  uint32_t round;        // rounds completed (mbarrier phase parity)
+};
+
+// Rows of the staging buffer for a trailing matrix of R rows: at least one
+// full M = 128 tile, and every column chunk a multiple of 16 rows.
+__host__ __device__ __forceinline__ int tc_rows_pad(int R) {
+  const int r16 = (R + 15) & ~15;
+  return r16 > 128 ? r16 : 128;
+}
+// Shared-memory bytes of the staging buffer of a matrix of order n (step 0
+// has the largest trailing matrix).
+__host__ __device__ __forceinline__ size_t tc_stage_bytes(int n) {
+  return n > PNB ? (size_t)3 * tc_rows_pad(n - PNB) * 64 : 0;
+}
+
+struct TcChunk {
+  int m0, own_lo, own_hi, c0, nc;
+};
+
+// Enumerate the (row tile, column chunk) pairs of a trailing matrix of R rows
+// in a fixed order; returns the number of pairs, fills `out` when non-null.
+__device__ __forceinline__ int tc_chunk(int R, int idx, TcChunk *out) {
+  const int ntiles = (R + 127) >> 7;
+  int k = 0;
+  for (int tile = 0; tile < ntiles; tile++) {
+    const int last = (tile == ntiles - 1);
+    int m0 = tile * 128;
+    if (last && R > 128) m0 = min(m0, ((R - 128) + 7) & ~7);
+    const int own_lo = tile * 128, own_hi = last ? R : (tile + 1) * 128;
+    const int N = (own_hi + 15) & ~15;
+    for (int c0 = 0; c0 < N; c0 += 256, k++) {
+      if (k == idx && out) {
+        out->m0 = m0;
+        out->own_lo = own_lo;
+        out->own_hi = own_hi;
+        out->c0 = c0;
+        out->nc = min(256, N - c0);
+      }
+    }
+  }
+  return k;
+}
+
+// Called by warps 1.. of a team that is the whole CTA (t.nt threads, t.nt >=
+// 64), for step p < np - 1. Skips the next panel's diagonal block (rows and
+// columns 0..31 of the trailing matrix): warp 0 updates it. Returns false if a
+// bounded wait ran out (tc.abort is then set).
+static __device__ bool team_trailing_tc(const Team &t, const PanelLayout &L, int p, float *Ps, TcCtx &tc)
+{
+  const int J = p * PNB, ld = L.ldp(p);
+  const float *Pp = Ps + L.base(p);
+  const int R = L.n - J - PNB;
+  const int rows_pad = tc_rows_pad(R);
+  const int utid = t.tid - 32, unt = t.nt - 32;
+  const int w = t.warp();  // 1 .. nwarps-1
+  const uint32_t term_bytes = (uint32_t)rows_pad * 64;
+  // 1. stage the three BF16 terms of P (rows past R are zero)
+  for (int e = utid; e < rows_pad * 4; e += unt) {
+    const int k8 = e / rows_pad, i = e - k8 * rows_pad;
+    uint32_t h[4], m[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const float x0 = (i < R) ? Pp[(PNB + i) + (size_t)(8 * k8 + 2 * q) * ld] : 0.f;
+      const float x1 = (i < R) ? Pp[(PNB + i) + (size_t)(8 * k8 + 2 * q + 1) * ld] : 0.f;
+      __nv_bfloat16 h0, m0, l0, h1, m1, l1;
+      bf16_split3(x0, h0, m0, l0);
+      bf16_split3(x1, h1, m1, l1);
+      h[q] = pack_bf16(h0, h1);
+      m[q] = pack_bf16(m0, m1);
+      l[q] = pack_bf16(l0, l1);
+    }
+    const uint32_t off = (uint32_t)(i >> 3) * TC_SBO + (uint32_t)k8 * TC_LBO + (uint32_t)(i & 7) * 16;
+    *reinterpret_cast<uint4 *>(tc.stage + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(tc.stage + term_bytes + off) = make_uint4(m[0], m[1], m[2], m[3]);
+    *reinterpret_cast<uint4 *>(tc.stage + 2 * term_bytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+  fence_async_smem();
+  asm volatile("bar.sync 15, %0;" ::"r"(unt) : "memory");
+  // 2. rounds of MMAs + epilogue
+  const int nchunks = tc_chunk(R, -1, nullptr);
+  const uint32_t sbase = smem_addr(tc.stage);
+  const int qd = w & 3;                     // TMEM lane quadrant of this warp
+  const int nq = (qd == 0) ? 1 : 2;         // warps sharing it among warps 1..7
+  const int qi = (qd == 0) ? 0 : (w >> 2);  // this warp's share
+  // products (A term, B term), 0 = hi, 1 = mid, 2 = lo: the small ones first
+  // and hi * hi last, so that the accumulator's alignment of each new partial
+  // sum to the running total costs bits only at the final, large magnitude
+  const int pa[6] = {1, 2, 0, 1, 0, 0}, pb[6] = {1, 0, 2, 0, 1, 0};
+  bool ok = true;
+  int c_first = 0;
+  while (c_first < nchunks) {
+    // chunks [c_first, c_end) fill at most TC_TMEM_COLS columns
+    int c_end = c_first, cols = 0;
+    while (c_end < nchunks) {
+      TcChunk ch;
+      tc_chunk(R, c_end, &ch);
+      if (cols + ch.nc > TC_TMEM_COLS) break;
+      cols += ch.nc;
+      c_end++;
+    }
+    if (utid == 0) {
+      tc_fence_after_sync();
+      int tcol = 0;
+      for (int c = c_first; c < c_end; c++) {
+        TcChunk ch;
+        tc_chunk(R, c, &ch);
+        const uint32_t idesc = idesc_bf16_f32(128, ch.nc);
+#pragma unroll
+        for (int s = 0; s < 6; s++) {
+#pragma unroll
+          for (int hh = 0; hh < 2; hh++) {
+            const uint32_t a = sbase + pa[s] * term_bytes + (uint32_t)(ch.m0 >> 3) * TC_SBO + hh * 256;
+            const uint32_t b = sbase + pb[s] * term_bytes + (uint32_t)(ch.c0 >> 3) * TC_SBO + hh * 256;
+            tc_mma_bf16(tc.tmem + tcol, smem_desc(a, TC_LBO, TC_SBO), smem_desc(b, TC_LBO, TC_SBO),
+                        idesc, (s | hh) ? 1u : 0u);
+          }
+        }
+        tcol += ch.nc;
+      }
+      tc_commit(tc.bar);
+    }
+    const bool done = mbar_wait_bounded(tc.bar, tc.round & 1u);
+    tc.round++;
+    if (!done) {
+      ok = false;
+      *tc.abort = 1;
+      if (tc.status) atomicExch(tc.status, 1);
+    }
+    tc_fence_after_sync();
+    if (done) {
+      int tcol = 0;
+      for (int c = c_first; c < c_end; c++) {
+        TcChunk ch;
+        tc_chunk(R, c, &ch);
+        const int wlo = ch.m0 + 32 * qd;  // rows [wlo, wlo + 32) are this warp's lanes
+        const int row = wlo + t.lane();
+        const bool rok = row >= ch.own_lo && row < ch.own_hi && row < R;
+        if (wlo + 32 > ch.own_lo && wlo < ch.own_hi && wlo < R) {
+          for (int g = qi; g * 16 < ch.nc; g += nq) {
+            const int cc = ch.c0 + g * 16;  // first trailing column of the group
+            if (cc > wlo + 31) break;       // the rest lies above the diagonal
+            if (wlo + 32 <= PNB && cc + 16 <= PNB) continue;  // warp 0's block
+            float v[16];
+            tmem_ld16(tc.tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(tcol + g * 16), v);
+            const int q = p + 1 + (cc >> 5);
+            float *Pq = Ps + L.base(q);
+            const int ldq = L.ldp(q);
+            const int rq = row - 32 * (cc >> 5);  // row inside panel q
+            if (rok) {
+#pragma unroll
+              for (int j = 0; j < 16; j++) {
+                const int col = cc + j;
+                if (col <= row && !(row < PNB && col < PNB))
+                  Pq[rq + (size_t)(col & 31) * ldq] -= v[j];
+              }
+            }
+          }
+        }
+        tcol += ch.nc;
+      }
+    }
+    tc_fence_before_sync();
+    asm volatile("bar.sync 15, %0;" ::"r"(unt) : "memory");
+    c_first = c_end;
+  }
+  return ok;
+}
+
 // Panel Cholesky with look-ahead, for teams of at least two warps: while
 // warps 1.. apply the trailing update of step p, warp 0 updates the next
 // diagonal block first and factors it, so the 32-step dependent chain of each
@@ -377,9 +605,12 @@ __device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T 
 // team. Ld2 holds two row-major 32 x LDD copies (current and next block).
 // INV: afterwards every diagonal square is replaced by its inverse (lower)
 // and the transpose of the inverse (strict upper), one block per warp.
+// tc (FP32 only, a team that is the whole CTA): the trailing update of warps
+// 1.. runs on the tensor cores (team_trailing_tc); returns -1 if one of its
+// bounded waits ran out.
 template <typename T, bool CHECK_INF, bool INV>
 __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T *Ld2, T *rinv,
-                                   T tol, int *flag)
+                                   T tol, int *flag, TcCtx *tc = nullptr)
 {
   const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
   KGB_SUBPHASE_BEGIN(t);
@@ -432,27 +663,18 @@ __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T
         __syncwarp();
         warp_factor_diag<T, CHECK_INF>(L, q, Ps, Ld2 + (q & 1) * 32 * LDD, rinv, tol, flag);
       }
-    } else {
-      const int utid = t.tid - 32, unt = t.nt - 32;
-      int tile0 = 0;
-      for (int q = p + 1; q < L.np; q++) {
-        const int K = q * PNB, mq = L.n - K, jq = L.jb(q);
-        const int rt = (mq + 3) >> 2, ct = (jq + 3) >> 2;
-        const int ntile = rt * ct;
-        T *Pq = Ps + L.base(q);
-        const int ldq = L.ldp(q);
-        const int start = ((utid - tile0) % unt + unt) % unt;
-        for (int tt = start; tt < ntile; tt += unt) {
-          const int c4 = tt / rt, r4 = tt - c4 * rt;
-          if (q == p + 1 && r4 < 8) continue;  // the next diagonal block: warp 0
-          if (r4 * 4 + 3 < c4 * 4) continue;
-          panel_tile_update<T>(Pp, ld, jb, K - J, r4 * 4, c4 * 4, Pq, ldq, jq);
-        }
-        tile0 += ntile;
+    } else if constexpr (sizeof(T) == 4) {
+      if (tc && p + 1 < L.np) {
+        team_trailing_tc(t, L, p, reinterpret_cast<float *>(Ps), *tc);
+      } else {
+        trailing_update_ffma<T>(t, L, p, Ps);
       }
+    } else {
+      trailing_update_ffma<T>(t, L, p, Ps);
     }
     t.sync();
     KGB_SUBPHASE_MARK(t, 10);
+    if (tc && *tc->abort) return -1;
     fail = *flag;
   }
   if (INV && !fail) {

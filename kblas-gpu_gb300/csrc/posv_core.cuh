@@ -74,7 +74,30 @@ struct PosvCfg {
   int nmax[PC_NCLS];  // class c holds n <= nmax[c] (ascending)
   int ts[PC_NCLS];    // team size (threads) of class c
   int spi[PC_NCLS];   // systems per work item of class c
+  float route_c;      // conditioning routing constant (route_fp64); <= 0: no routing
 };
+
+// Routing to FP64 before any refinement, from a conditioning estimate that
+// the FP32 factorization gives for free. On the scaled matrix (unit
+// diagonal) every pivot d_i = L_ii^2 lies in [lambda_min, lambda_max], so
+// d_min = min d_i bounds lambda_min from above; the refinement contracts the
+// error by about rho = ||A^-1 dA|| with ||dA|| ~ c u32 (u32 = 2^-24), so
+// rho_hat = c u32 / d_min. From the first FP32 solve's backward error (~
+// sqrt(n) u32) to the target (9n - 2) u64 takes
+// k = log2(sqrt(n) u32 / ((9n - 2) u64)) / -log2(rho_hat) refinement steps,
+// each one FP64 residual sweep (n^2 nr FMAs) after the first, against n^3 / 6
+// + n^2 nr for the FP64 factor and solve: a system goes straight to the FP64
+// path when rho_hat >= 1/2 or k > n / (6 nr). The refinement's own cost-model
+// exit (refine_too_slow) still catches what the estimate misses.
+__device__ __forceinline__ bool route_fp64(float dmin, int n, int nr, float c) {
+  if (!(c > 0.f)) return false;
+  if (!(dmin > 0.f)) return true;
+  const float rho = c * 5.9604645e-08f / dmin;
+  if (!(rho < 0.5f)) return true;
+  const float l = 29.0f + 0.5f * log2f((float)n) - log2f(9.0f * n - 2.0f);
+  const float k = l / -log2f(rho);
+  return k > (float)n / (6.0f * (float)nr);
+}
 
 __host__ __device__ __forceinline__ int pc_class(const PosvCfg &c, int n) {
   for (int k = 0; k < PC_NCLS; k++)
@@ -123,13 +146,19 @@ struct OutArgs {
   int *iter;
   char *scratch;         // per-CTA global scratch slots
   long long slot_bytes;
+  int tc;                // mixed panel path: tensor-core trailing updates for whole-CTA teams
+  int *status;           // device status word: set to 1 when a bounded wait ran out (may be null)
 };
 
 // ---------------------------------------------------------------------------
 // shared-memory bytes of one team
 // ---------------------------------------------------------------------------
+// tc: a whole-CTA team of the mixed panel path stages the BF16 operands of
+// its tensor-core trailing updates in the region of the solve / refinement
+// vectors (free during the factorization), grown to the staging size.
 template <bool MIXED>
-__host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool fac_in_smem) {
+__host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool fac_in_smem,
+                                                           bool tc = false) {
   if (n <= 32) {
     // register path: row-major L (FP64; FP32 too for mixed), reciprocal
     // pivots, scales
@@ -147,10 +176,13 @@ __host__ __device__ __forceinline__ size_t team_smem_bytes(int n, int ts, bool f
   b += (size_t)n * 8;                              // rinv (FP64 size: fallback too)
   if (MIXED) {
     b += (size_t)n * 8;                            // scales + exponent shifts
-    b += (size_t)PC_MR * n * 4;                    // FP32 solve vectors
-    b = (b + 7) / 8 * 8;
-    b += 2 * (size_t)PC_MR * n * 8;                // x, r
-    b += (size_t)nw * n * 8;                       // per-warp column sums of the residual
+    b = (b + 15) / 16 * 16;
+    size_t u = (size_t)PC_MR * n * 4;              // FP32 solve vectors
+    u = (u + 7) / 8 * 8;
+    u += 2 * (size_t)PC_MR * n * 8;                // x, r
+    u += (size_t)nw * n * 8;                       // per-warp column sums of the residual
+    if (tc && ts == PC_NT && u < tc_stage_bytes(n)) u = tc_stage_bytes(n);
+    b += u;
   } else {
     b += (size_t)n * 8;                            // solve vector
   }
@@ -229,7 +261,7 @@ __device__ int small_fp64_posv(bool active, int n, int m, int r_from, double *A,
 
 template <int W>
 __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, double *B, int ldb,
-                                 unsigned char *base, int *info_out, int *iter_out)
+                                 unsigned char *base, int *info_out, int *iter_out, float route_c)
 {
   const int lane = threadIdx.x & (W - 1);
   double *Ls64 = reinterpret_cast<double *>(base);
@@ -261,6 +293,14 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
   const int any_bad = seg_any(bad, W);
   bool need_fb = active && (fail != 0 || any_bad);
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
+  {
+    // conditioning routing (every lane of the warp runs the shuffles)
+    const float rmax = warp_max_width((lane < n) ? rinv[lane] : 0.f, W);
+    if (active && !need_fb && route_fp64(1.0f / (rmax * rmax), n, max(m, 1), route_c)) {
+      need_fb = true;
+      fb_code = -4;
+    }
+  }
   const double tol_conv = posv_eta_target(n);
   const int m_hi = warp_uniform_max_w(active ? m : 0, W);
   for (int r0 = 0; r0 < m_hi; r0++) {
@@ -428,10 +468,13 @@ static __device__ void panel_plain_potrs(const Team &t, int n, int m, const doub
 // global scratch slot). A compile-time choice, so that every access to a
 // shared-memory factor compiles to a shared-memory instruction rather than a
 // generic one.
+// tc (a team that is the whole CTA, else null): tensor-core trailing updates,
+// operands staged in the solve / refinement region.
 template <bool FAC_SMEM>
 static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, int lda, double *B,
                                  int ldb, unsigned char *base, float *Ps_scratch,
-                                 double *Ps64_scratch, int *info_out, int *iter_out)
+                                 double *Ps64_scratch, int *info_out, int *iter_out, TcCtx *tc,
+                                 float route_c)
 {
   const PanelLayout L = make_layout(n);
   const int nw = t.nwarps();
@@ -443,11 +486,15 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   float *rinv = reinterpret_cast<float *>(rinv64);
   float *scl = reinterpret_cast<float *>(p); p += (size_t)n * 4;
   int *sh = reinterpret_cast<int *>(p); p += (size_t)n * 4;
+  p = base + (((size_t)(p - base) + 15) & ~(size_t)15);  // offset arithmetic keeps p shared
+  unsigned char *region = p;  // ys, x, r, colsum; or the tensor-core staging
   float *ys = reinterpret_cast<float *>(p); p += (size_t)PC_MR * n * 4;
-  p = base + (((size_t)(p - base) + 7) & ~(size_t)7);  // offset arithmetic keeps p shared
+  p = base + (((size_t)(p - base) + 7) & ~(size_t)7);
   double *x = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
   double *r = reinterpret_cast<double *>(p); p += (size_t)PC_MR * n * 8;
   double *colsum = reinterpret_cast<double *>(p); p += (size_t)nw * n * 8;
+  if (tc && (size_t)(p - region) < tc_stage_bytes(n)) p = region + tc_stage_bytes(n);
+  if (tc) tc->stage = region;
   double *red = reinterpret_cast<double *>(p); p += (size_t)32 * nw * 8;
   int *flag = reinterpret_cast<int *>(p);
   KGB_PHASE_BEGIN(t);
@@ -470,12 +517,22 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
   double anorm = -1.0;
   const float ftol = (float)n * 5.9604645e-08f;  // n * 2^-24
   const int fail = (t.nt >= 64)
-                       ? team_potrf_panel_la<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag)
+                       ? team_potrf_panel_la<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag, tc)
                        : team_potrf_panel<float, true, true>(t, L, Ps, Ld, rinv, ftol, flag, true);
   KGB_PHASE_MARK(t, 1);
+  if (fail < 0) return;  // a tensor-core wait ran out: the launch stops, nothing is written
   const int any_bad = team_any(t, bad, reinterpret_cast<int *>(red));
   bool need_fb = fail != 0 || any_bad;
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
+  if (!need_fb && route_c > 0.f) {
+    float rl = 0.f;
+    for (int i = t.tid; i < n; i += t.nt) rl = fmaxf(rl, rinv[i]);
+    const float rmax = team_max<float>(t, rl, reinterpret_cast<float *>(red));
+    if (route_fp64(1.0f / (rmax * rmax), n, max(m, 1), route_c)) {
+      need_fb = true;
+      fb_code = -4;
+    }
+  }
   const double tol_conv = posv_eta_target(n);
   // 3. solve + refine, PC_MR right-hand sides at a time
   for (int r0 = 0; r0 < m && !need_fb; r0 += PC_MR) {
@@ -621,6 +678,27 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
 {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_item;
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_tcbar;
+  __shared__ int s_abort;
+  // tensor-core trailing updates (mixed panel path): the CTA holds all TMEM
+  // columns for the whole launch (one CTA per SM) and one mbarrier
+  const bool use_tc = MIXED && (PATHS & 2) != 0 && out.tc != 0;
+  if (use_tc) {
+    if (threadIdx.x < 32) {
+      tmem_alloc(&s_tmem, TC_TMEM_COLS);
+      tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+      mbar_init(&s_tcbar, 1);
+      mbar_init_fence();
+      s_abort = 0;
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+  }
+  TcCtx tcx{use_tc ? s_tmem : 0u, &s_tcbar, nullptr, &s_abort, out.status, 0u};
   long long first = 0, nitems;
   if (it.uniform) {
     const int spi = cfg.spi[pc_class(cfg, it.n_uniform)];
@@ -636,8 +714,9 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
   for (;;) {
     __syncthreads();
     const long long q = s_item;
+    const bool stop = use_tc && s_abort != 0;
     __syncthreads();
-    if (q >= nitems) break;
+    if (q >= nitems || stop) break;
     // claim the next item now and warm L2 with its matrices
     if (threadIdx.x == 0) s_item = (int)first + atomicAdd(it.queue, 1);
     __syncthreads();
@@ -648,8 +727,10 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
     const int TS = cfg.ts[c];
     const int team_id = threadIdx.x / TS;
     const int nteams = PC_NT / TS;
-    const bool fac_smem = (size_t)nteams * team_smem_bytes<MIXED>(n, TS, true) <= (size_t)smem_bytes;
-    const size_t tb = team_smem_bytes<MIXED>(n, TS, fac_smem);
+    const bool item_tc = use_tc && nteams == 1 && n > 32;
+    const bool fac_smem =
+        (size_t)nteams * team_smem_bytes<MIXED>(n, TS, true, item_tc) <= (size_t)smem_bytes;
+    const size_t tb = team_smem_bytes<MIXED>(n, TS, fac_smem, item_tc);
     const bool active = team_id < count;
     long long sidx = 0;
     int m = 0, lda = 1, ldb = 1;
@@ -666,7 +747,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
       // register path: every segment of each warp runs, idle ones on no data
 #define KGB_SMALL(WW)                                                                      \
   if (MIXED) {                                                                             \
-    small_mixed_posv<WW>(active, n, m, A, lda, B, ldb, base, info_p, iter_p);              \
+    small_mixed_posv<WW>(active, n, m, A, lda, B, ldb, base, info_p, iter_p, cfg.route_c); \
   } else {                                                                                 \
     double *ls_ = reinterpret_cast<double *>(base);                                        \
     const int inf_ = small_fp64_posv<WW>(active, n, m, 0, A, lda, B, ldb, ls_,             \
@@ -693,10 +774,13 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
                                (size_t)team_id * L.total()
                          : nullptr;
       if (MIXED) {
+        TcCtx *tcp = item_tc ? &tcx : nullptr;
         if (fac_smem)
-          panel_mixed_posv<true>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p);
+          panel_mixed_posv<true>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p, tcp,
+                                 cfg.route_c);
         else
-          panel_mixed_posv<false>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p);
+          panel_mixed_posv<false>(t, n, m, A, lda, B, ldb, base, P32s, P64s, info_p, iter_p, tcp,
+                                  cfg.route_c);
       } else {
         if (sys.op == 2) {
           if (fac_smem)
@@ -712,6 +796,13 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
       }
     }
     __syncthreads();
+  }
+  if (use_tc) {
+    // every MMA was waited for (or its wait ran out and the loop stopped)
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    if (threadIdx.x < 32) tmem_dealloc(s_tmem, TC_TMEM_COLS);
   }
 }
 

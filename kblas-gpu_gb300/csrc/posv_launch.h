@@ -2,6 +2,7 @@
 // launch shape per size class, shared-memory budget, grid, workspace layout.
 #pragma once
 
+#include <stdlib.h>
 #include <string.h>
 
 #include "kblas_internal.h"
@@ -19,13 +20,26 @@ struct PosvPlan {
   int smem = 0;           // dynamic shared memory per CTA
   int grid = 0;           // persistent CTAs
   size_t slot_bytes = 0;  // global scratch per CTA
+  int tc = 0;             // mixed panel path: tensor-core trailing updates for whole-CTA teams
 };
+
+// Tensor-core trailing updates are used by the mixed panel path when a size
+// class in range runs one team per CTA (the team then owns all of the SM's
+// TMEM) and, with the BF16 staging buffer, every class still fits the
+// shared-memory budget with one CTA per SM. KGB_NO_TC=1 in the environment
+// turns them off (FP32 FMA updates), for comparisons.
+static inline bool tc_disabled_by_env() {
+  const char *e = getenv("KGB_NO_TC");
+  return e && e[0] == '1';
+}
 
 // Process-wide override of the tuning table (set by the autotuner through
 // kblasSetPosvTuning); zero entries mean "use the compiled table".
 struct TuneOverride {
   int set[2] = {0, 0};
   PosvCfg cfg[2];
+  int route_set = 0;
+  float route_c = 0.f;
 };
 TuneOverride &tune_override();
 
@@ -39,12 +53,15 @@ static inline PosvCfg default_cfg(bool mixed) {
     c.spi[k] = mixed ? ms[k] : ps[k];
   }
   c.nmax[PC_NCLS - 1] = PC_MAX_N;
+  c.route_c = KGB_TUNE_ROUTE_C;
   return c;
 }
 
 static inline PosvCfg current_cfg(bool mixed) {
   TuneOverride &o = tune_override();
-  return o.set[mixed ? 1 : 0] ? o.cfg[mixed ? 1 : 0] : default_cfg(mixed);
+  PosvCfg c = o.set[mixed ? 1 : 0] ? o.cfg[mixed ? 1 : 0] : default_cfg(mixed);
+  c.route_c = o.route_set ? o.route_c : KGB_TUNE_ROUTE_C;
+  return c;
 }
 
 // A class whose orders are all <= 32 runs the register path: team size W in
@@ -73,25 +90,42 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
   pl.cfg = current_cfg(MIXED);
   if (!cfg_valid(pl.cfg)) return KBLAS_WrongConfig;
   const size_t budget = (size_t)(max_smem(h) < (int)PC_SMEM_BUDGET ? max_smem(h) : (int)PC_SMEM_BUDGET);
-  size_t smem = 0;
-  for (int c = 0; c < PC_NCLS; c++) {
-    const int nlo = c ? pl.cfg.nmax[c - 1] + 1 : 1;
-    const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
-    if (nhi < nlo) continue;
-    const int nteams = PC_NT / pl.cfg.ts[c];
-    size_t b = 0;
-    if ((PATHS & 1) && nlo <= 32) {
-      const size_t b1 = (size_t)nteams * team_smem_bytes<MIXED>(nhi < 32 ? nhi : 32, pl.cfg.ts[c], true);
-      if (b1 > b) b = b1;
+  // shared memory of the launch: the largest need over the classes in range
+  auto need = [&](bool tc, size_t &out) -> bool {
+    size_t smem = 0;
+    for (int c = 0; c < PC_NCLS; c++) {
+      const int nlo = c ? pl.cfg.nmax[c - 1] + 1 : 1;
+      const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
+      if (nhi < nlo) continue;
+      const int nteams = PC_NT / pl.cfg.ts[c];
+      size_t b = 0;
+      if ((PATHS & 1) && nlo <= 32) {
+        const size_t b1 = (size_t)nteams * team_smem_bytes<MIXED>(nhi < 32 ? nhi : 32, pl.cfg.ts[c], true);
+        if (b1 > b) b = b1;
+      }
+      if ((PATHS & 2) && nhi > 32) {
+        const bool ctc = tc && nteams == 1;
+        size_t b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], true, ctc);
+        if (b2 > budget) b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], false, ctc);
+        if (b2 > b) b = b2;
+      }
+      if (b > budget) return false;
+      if (b > smem) smem = b;
     }
-    if ((PATHS & 2) && nhi > 32) {
-      size_t b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], true);
-      if (b2 > budget) b2 = (size_t)nteams * team_smem_bytes<MIXED>(nhi, pl.cfg.ts[c], false);
-      if (b2 > b) b = b2;
+    out = smem;
+    return true;
+  };
+  bool want_tc = false;
+  if (MIXED && (PATHS & 2) && !tc_disabled_by_env()) {
+    for (int c = 0; c < PC_NCLS; c++) {
+      const int nlo = c ? pl.cfg.nmax[c - 1] + 1 : 1;
+      const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
+      if (nhi >= nlo && nhi > 32 && pl.cfg.ts[c] == PC_NT) want_tc = true;
     }
-    if (b > budget) return KBLAS_NotSupported;
-    if (b > smem) smem = b;
   }
+  size_t smem = 0;
+  if (want_tc && !need(true, smem)) want_tc = false;
+  if (!want_tc && !need(false, smem)) return KBLAS_NotSupported;
   if (smem == 0) smem = 16;
   pl.smem = (int)smem;
   auto kern = posv_persistent_kernel<MIXED, PATHS>;
@@ -101,6 +135,18 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, smem) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
+  // a CTA with tensor-core updates takes every TMEM column of its SM
+  if (want_tc && per_sm > 1) {
+    if (!need(false, smem)) return KBLAS_NotSupported;
+    want_tc = false;
+    pl.smem = (int)(smem ? smem : 16);
+    st = set_smem(kern, pl.smem);
+    if (st != KBLAS_Success) return st;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, pl.smem) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+  }
+  pl.tc = want_tc ? 1 : 0;
   pl.grid = h->sm_count * per_sm;
   pl.slot_bytes = (PATHS & 2) ? posv_slot_bytes(pl.cfg, max_n) : 0;
   return KBLAS_Success;

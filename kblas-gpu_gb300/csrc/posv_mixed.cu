@@ -58,7 +58,7 @@ static int mixed_uniform(KBlasHandle *h, char side, char uplo, int m, int n, Sys
   it.batch = batch;
   it.n_uniform = n;
   it.queue = header;
-  OutArgs out{info, iter, base + ws.scratch, (long long)pl.slot_bytes};
+  OutArgs out{info, iter, base + ws.scratch, (long long)pl.slot_bytes, pl.tc, h->d_status};
   sys.n = n;
   sys.m = m;
   if (n > 32)
@@ -128,7 +128,8 @@ int mixed_uniform_fixed_scratch(cudaStream_t stream, int device, int sm_count, i
   it.batch = batch;
   it.n_uniform = n;
   it.queue = header;
-  OutArgs out{info, iter, pl.slot_bytes ? scratch + head : nullptr, (long long)pl.slot_bytes};
+  OutArgs out{info, iter, pl.slot_bytes ? scratch + head : nullptr, (long long)pl.slot_bytes,
+              pl.tc, nullptr};
   if (n > 32)
     posv_persistent_kernel<true, 2><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
   else
@@ -190,9 +191,25 @@ int kblasSetPosvTuning(int mixed, const int *nmax, const int *ts, const int *spi
     c.spi[i] = spi[i];
   }
   c.nmax[PC_NCLS - 1] = PC_MAX_N;
+  c.route_c = 0.f;  // taken from the routing override or the compiled constant
   if (!cfg_valid(c)) return KBLAS_Error_WrongInput;
   o.cfg[k] = c;
   o.set[k] = 1;
+  return KBLAS_Success;
+}
+
+// Conditioning routing constant of the mixed-precision POSV (the constant c
+// of the estimate rho = c * 2^-24 / d_min, see route_fp64): c > 0 sets it,
+// c == 0 turns the routing off, c < 0 restores the compiled constant.
+int kblasSetPosvRouting(double c) {
+  TuneOverride &o = tune_override();
+  if (c != c) return KBLAS_Error_WrongInput;
+  if (c < 0.0) {
+    o.route_set = 0;
+  } else {
+    o.route_set = 1;
+    o.route_c = (float)c;
+  }
   return KBLAS_Success;
 }
 

@@ -144,7 +144,8 @@ int fp64_uniform_persistent(KBlasHandle *h, int op, int m, int n, SysArgs sys, i
   it.batch = batch;
   it.n_uniform = n;
   it.queue = header;
-  OutArgs out{op == 2 ? nullptr : info, nullptr, base + ws.scratch, (long long)pl.slot_bytes};
+  OutArgs out{op == 2 ? nullptr : info, nullptr, base + ws.scratch, (long long)pl.slot_bytes,
+              0, h->d_status};
   posv_persistent_kernel<false, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
   KGB_LAUNCH_CHECK("posv_persistent_kernel<fp64>");
   return KBLAS_Success;
@@ -208,7 +209,8 @@ static int vbatch(KBlasHandle *h, char side, char uplo, int *m, int *n, int max_
   it.perm = perm;
   it.nitems_p = header + 1;
   it.split_p = header + 3;
-  OutArgs out{info, MIXED ? iter : nullptr, base + ws.scratch, (long long)pl.slot_bytes};
+  OutArgs out{info, MIXED ? iter : nullptr, base + ws.scratch, (long long)pl.slot_bytes,
+              pl.tc, h->d_status};
   // orders > 32 first (largest first), then orders <= 32 on the register path
   if (max_n > 32) {
     it.queue = header;

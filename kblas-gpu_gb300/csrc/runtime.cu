@@ -164,7 +164,7 @@ const char *kblasGetErrorString(int error) {
     case KBLAS_Error_WrongInput: return "One of input parameter's value is wrong";
     case KBLAS_MAGMA_Error: return "MAGMA error";
     case KBLAS_SVD_NoConvergence: return "SVD-gram operation did not converge.";
-    case KBLAS_Error_Timeout: return "A bounded device-side wait ran out";
+    case KBLAS_Error_Timeout: return "A bounded device-side wait for the tensor cores ran out";
     default: return "unknown KBLAS error code";
   }
 }
@@ -216,10 +216,15 @@ int kblasAllocateWorkspace(kblasHandle_t h) {
 
 int kblas_roundup(int x, int y) { return (x + y - 1) / y * y; }
 
+// The handle's device status word is set by the mixed-precision persistent
+// kernels when a bounded wait for their tensor-core MMAs runs out (the kernel
+// then stops without writing results). It stays set until read here; reading
+// clears it.
 int kblasGetDeviceStatus(kblasHandle_t h) {
   if (!h) return KBLAS_Error_NotInitialized;
   int s = 0;
   if (cudaMemcpyAsync(&s, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess)
     return KBLAS_CUDA_Error;
   return s == 0 ? KBLAS_Success : KBLAS_Error_Timeout;

@@ -10,6 +10,9 @@
 #define KGB_TUNE_MIXED_TS {8, 16, 32, 32, 64, 32, 128, 256}
 #define KGB_TUNE_MIXED_SPI {32, 16, 8, 8, 4, 8, 2, 1}
 
+// conditioning routing constant of the mixed path (route_fp64)
+#define KGB_TUNE_ROUTE_C 8.0f
+
 #define KGB_TUNE_PLAIN_NMAX {8, 16, 32, 64, 96, 128, 176, 1024}
 #define KGB_TUNE_PLAIN_TS {8, 16, 32, 32, 32, 32, 64, 64}
 #define KGB_TUNE_PLAIN_SPI {32, 16, 8, 8, 8, 8, 4, 4}

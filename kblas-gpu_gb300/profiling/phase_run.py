@@ -12,7 +12,9 @@ tail (write-back). Sub-phases of the factorization (chol_panel.cuh,
 team_potrf_panel_la): f:diag0, f:rows_trsm, f:trailing, f:invert.
 
 Run on the GPU:  python kblas-gpu_gb300/profiling/phase_build.py &&
-                 python kblas-gpu_gb300/profiling/phase_run.py [batch n nrhs]
+                 python kblas-gpu_gb300/profiling/phase_run.py [batch n nrhs [sqexp|spd]]
+(KGB_NO_TC=1 in the environment: FP32 FMA trailing updates instead of the
+tensor cores, for comparison.)
 """
 import ctypes as C
 import importlib.util
@@ -48,8 +50,12 @@ def main():
     batch = int(sys.argv[1]) if len(sys.argv) > 1 else 2000
     n = int(sys.argv[2]) if len(sys.argv) > 2 else 512
     m = int(sys.argv[3]) if len(sys.argv) > 3 else 8
+    kind = sys.argv[4] if len(sys.argv) > 4 else "sqexp"
     prop = torch.cuda.get_device_properties(0)
-    a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range((batch + 99) // 100)])[:batch]
+    if kind == "spd":  # A = G G^T + n I (the variable-size benchmark's recipe)
+        a = wl.spd_shifted(batch, n, seed=0)
+    else:
+        a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range((batch + 99) // 100)])[:batch]
     b = wl.rhs_rows(batch, m, n, seed=1)
     A0, B0 = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     A, B = A0.clone(), B0.clone()
@@ -81,7 +87,8 @@ def main():
     lib.kgb_phase_all(buf, 0)
     itv = it.cpu().numpy()
     clock_hz = 2.07e9  # the maximum SM clock; the benchmark's clock samples show it held
-    out = {"batch": batch, "n": n, "nrhs": m, "ms": ms,
+    out = {"batch": batch, "n": n, "nrhs": m, "matrices": kind, "ms": ms,
+           "tensor_core_update": os.environ.get("KGB_NO_TC") != "1",
            "per_sm_cycles_per_system": ms * 1e-3 * clock_hz * prop.multi_processor_count / batch,
            "mean_steps": float(itv[itv >= 0].mean()) if (itv >= 0).any() else None,
            "fallbacks": int((itv < 0).sum()), "phases": {}}

@@ -166,20 +166,33 @@ int oracle_max_threads(void)
 typedef void (*orc_lapack_dpotrf_fn)(char *, int *, double *, int *, int *);
 typedef void (*orc_lapack_dpotrs_fn)(char *, int *, int *, double *, int *, double *, int *, int *);
 
+void oracle_lapack_dposv_vbatch(void *potrf, void *potrs, const int *n, int nrhs,
+                                double *const *A, const int *lda, double *const *B,
+                                const int *ldb, int batch, int *info, int nthreads);
+
 void oracle_lapack_dposv1_vbatch(void *potrf, void *potrs, const int *n, double *const *A,
                                  const int *lda, double *const *B, int batch, int *info,
                                  int nthreads)
+{
+    oracle_lapack_dposv_vbatch(potrf, potrs, n, 1, A, lda, B, n, batch, info, nthreads);
+}
+
+/* The same with nrhs right-hand sides per system: B[b] is n x nrhs,
+ * column-major with leading dimension ldb[b] (LAPACK's layout). */
+void oracle_lapack_dposv_vbatch(void *potrf, void *potrs, const int *n, int nrhs,
+                                double *const *A, const int *lda, double *const *B,
+                                const int *ldb, int batch, int *info, int nthreads)
 {
     const orc_lapack_dpotrf_fn f = (orc_lapack_dpotrf_fn)potrf;
     const orc_lapack_dpotrs_fn s = (orc_lapack_dpotrs_fn)potrs;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
     for (int b = 0; b < batch; b++) {
         char lo = 'L';
-        int nn = n[b], ld = lda[b], one = 1, inf = 0;
+        int nn = n[b], ld = lda[b], nr = nrhs, inf = 0;
         if (nn > 0) f(&lo, &nn, A[b], &ld, &inf);
-        if (inf == 0 && nn > 0) {
-            int ldb = nn, inf2 = 0;
-            s(&lo, &nn, &one, A[b], &ld, B[b], &ldb, &inf2);
+        if (inf == 0 && nn > 0 && nr > 0) {
+            int lb = ldb[b], inf2 = 0;
+            s(&lo, &nn, &nr, A[b], &ld, B[b], &lb, &inf2);
         }
         info[b] = inf;
     }

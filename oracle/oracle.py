@@ -403,6 +403,31 @@ def host_lapack():
     return _lapack or None
 
 
+def lapack_posv_batch(A: np.ndarray, B: np.ndarray, nthreads=None):
+    """The host LAPACK's dpotrf + dpotrs over a uniform batch: A (batch, n, n)
+    column-major matrices (array [b, j, i] = a_ij), B (batch, nrhs, n), i.e.
+    each system's right-hand sides as n x nrhs column-major (LAPACK's layout).
+    OpenMP over the batch. Returns info, or None without a host LAPACK."""
+    lp = host_lapack()
+    if lp is None:
+        return None
+    L = lib()
+    f = L.oracle_lapack_dposv_vbatch
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+    f.restype = None
+    assert A.flags.c_contiguous and B.flags.c_contiguous and A.dtype == np.float64
+    batch, n = A.shape[0], A.shape[-1]
+    nrhs = B.shape[1]
+    nn = np.full(batch, n, dtype=np.int32)
+    pa = (A.ctypes.data + np.arange(batch, dtype=np.uint64) * np.uint64(A[0].nbytes)).astype(np.uint64)
+    pb = (B.ctypes.data + np.arange(batch, dtype=np.uint64) * np.uint64(B[0].nbytes)).astype(np.uint64)
+    info = np.zeros(batch, dtype=np.int32)
+    f(lp[0], lp[1], _p(nn), nrhs, _p(pa), _p(nn), _p(pb), _p(nn), batch, _p(info),
+      nthreads or nthreads_default())
+    return info
+
+
 def lapack_posv1_vbatch(ns, As, ldas, Bs, nthreads=None):
     """The host LAPACK's dpotrf + dpotrs over a variable-size batch (one
     right-hand side per system, Bs[b] holding n contiguous values), OpenMP
