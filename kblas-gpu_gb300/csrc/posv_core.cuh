@@ -88,7 +88,9 @@ struct PosvCfg {
 // each one FP64 residual sweep (n^2 nr FMAs) after the first, against n^3 / 6
 // + n^2 nr for the FP64 factor and solve: a system goes straight to the FP64
 // path when rho_hat >= 1/2 or k > n / (6 nr). The refinement's own cost-model
-// exit (refine_too_slow) still catches what the estimate misses.
+// exit (refine_too_slow) still catches what the estimate misses. Panel path
+// only (n > 32): below that the FP64 factorization is not the cheaper path
+// in practice (every step is latency, not FP64 work).
 __device__ __forceinline__ bool route_fp64(float dmin, int n, int nr, float c) {
   if (!(c > 0.f)) return false;
   if (!(dmin > 0.f)) return true;
@@ -261,7 +263,7 @@ __device__ int small_fp64_posv(bool active, int n, int m, int r_from, double *A,
 
 template <int W>
 __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, double *B, int ldb,
-                                 unsigned char *base, int *info_out, int *iter_out, float route_c)
+                                 unsigned char *base, int *info_out, int *iter_out)
 {
   const int lane = threadIdx.x & (W - 1);
   double *Ls64 = reinterpret_cast<double *>(base);
@@ -293,14 +295,6 @@ __device__ void small_mixed_posv(bool active, int n, int m, double *A, int lda, 
   const int any_bad = seg_any(bad, W);
   bool need_fb = active && (fail != 0 || any_bad);
   int fb_code = need_fb ? -1 : 0, fb_from = 0, steps_used = 0;
-  {
-    // conditioning routing (every lane of the warp runs the shuffles)
-    const float rmax = warp_max_width((lane < n) ? rinv[lane] : 0.f, W);
-    if (active && !need_fb && route_fp64(1.0f / (rmax * rmax), n, max(m, 1), route_c)) {
-      need_fb = true;
-      fb_code = -4;
-    }
-  }
   const double tol_conv = posv_eta_target(n);
   const int m_hi = warp_uniform_max_w(active ? m : 0, W);
   for (int r0 = 0; r0 < m_hi; r0++) {
@@ -747,7 +741,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
       // register path: every segment of each warp runs, idle ones on no data
 #define KGB_SMALL(WW)                                                                      \
   if (MIXED) {                                                                             \
-    small_mixed_posv<WW>(active, n, m, A, lda, B, ldb, base, info_p, iter_p, cfg.route_c); \
+    small_mixed_posv<WW>(active, n, m, A, lda, B, ldb, base, info_p, iter_p);              \
   } else {                                                                                 \
     double *ls_ = reinterpret_cast<double *>(base);                                        \
     const int inf_ = small_fp64_posv<WW>(active, n, m, 0, A, lda, B, ldb, ls_,             \

@@ -82,8 +82,39 @@ def test_mixed_illconditioned_cond_1e2_to_1e8(gpu, handle, kb, wl, orc):
         assert orc.factor_backward_error(a[s], A[s], n) <= 10 * n * EPS64
     conv = np.where(it >= 0)[0]
     assert np.array_equal(A[conv], a[conv])
-    # the well-conditioned part converges in a few steps
-    assert (it[cond < 1e4] >= 0).all()
+    # the well-conditioned part converges in a few steps; the worst part is
+    # routed to FP64 by the conditioning estimate before any refinement
+    assert (it[cond < 1e3] >= 0).all()
+    assert (it[cond > 1e7] == -4).any()
+
+
+def test_mixed_routing_off_and_on(gpu, handle, kb, wl, orc):
+    """kblasSetPosvRouting(0) turns the conditioning routing off (no iter -4;
+    the refinement's cost-model exit alone sends systems to FP64); a large
+    constant routes every system; each one meets the bar either way."""
+    n, m, batch = 64, 4, 96
+    a, cond = wl.spd_cond(batch, n, seed=13)
+    b = wl.rhs_rows(batch, m, n, seed=14)
+    L = kb.lib()
+    try:
+        counts = {}
+        for c in (0.0, 1e6):
+            assert L.kblasSetPosvRouting(c) == 1
+            A, X, info, it = run_uniform_mixed(gpu, kb, handle, a, b, m, n)
+            assert (info == 0).all()
+            eta = orc.backward_error_r(a, X, b, m, n)
+            assert eta.max() <= 10 * n * EPS64, (c, eta.max())
+            counts[c] = int((it == -4).sum())
+            if c == 0.0:
+                assert (it[cond < 1e4] >= 0).all()
+            else:
+                # every system whose FP32 pivots passed (-1 otherwise) is routed
+                assert set(np.unique(it).tolist()) <= {-1, -4}, np.unique(it)
+        assert counts[0.0] == 0
+        assert counts[1e6] > 0
+    finally:
+        assert L.kblasSetPosvRouting(-1.0) == 1
+    assert L.kblasSetPosvRouting(float("nan")) == kb.KBLAS_Error_WrongInput
 
 
 @pytest.mark.parametrize("n", [150, 300])
