@@ -258,7 +258,12 @@ def measure_fp64_peak(kb, torch):
         times.append(float(p.kblas_probe_fma(64, nsm, threads, iters, ilp, scratch.data_ptr())))
     flop = 2.0 * nsm * threads * iters * ilp
     best = max(flop / (ms * 1e-3) / 1e12 for ms in times)
+    # the same chains on 32, 16 and 8 lanes of each warp: the time barely
+    # moves, i.e. a predicated-off lane still costs its FP64 issue slot
+    lanes = {str(a): float(p.kblas_probe_fma64_lanes(nsm, threads, iters, a, scratch.data_ptr()))
+             for a in (32, 16, 8)}
     return {"peak_tflops_measured_live": best,
+            "predicated_lanes_probe_ms": lanes,
             "probe": {"kernel": "fma_chain_kernel<double, 4> (csrc/probe.cu)", "blocks": nsm,
                       "threads_per_block": threads, "ilp_chains_per_thread": ilp,
                       "fma_per_chain": iters, "flop_per_launch": flop, "repeats": repeats,
@@ -621,14 +626,15 @@ def cfg_posv_mixed(c, which, cpu_seconds=4.0):
     RHS, or the n = 512 covariances with 8 RHS."""
     torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
     if which == "mixed_posv_n64":
-        batch, n, m = 50_000, 64, 4
+        batch, n, m = min(50_000, c.args.batch), 64, 4
         a, cond = wl.spd_cond(batch, n, seed=0)
-        desc = ("mixed vs FP64 DPOSV, 50000 x n=64, cond log-uniform 1e2..1e8 (Q diag Q^T), "
+        desc = (f"mixed vs FP64 DPOSV, {batch} x n=64, cond log-uniform 1e2..1e8 (Q diag Q^T), "
                 "4 RHS, strided")
     else:
-        batch, n, m = 2_000, 512, 8
+        # --batch below 2000 shrinks the batch (whole hundreds), for profiler captures
+        batch, n, m = max(100, min(2_000, c.args.batch) // 100 * 100), 512, 8
         a = np.concatenate([wl.sqexp_cov(100, n, seed=k) for k in range(batch // 100)])
-        desc = ("mixed vs FP64 DPOSV, 2000 x n=512 squared-exponential covariances, "
+        desc = (f"mixed vs FP64 DPOSV, {batch} x n=512 squared-exponential covariances, "
                 "l ~ U[0.05, 0.3], nugget 1e-4, 8 RHS, strided")
     b = wl.rhs_rows(batch, m, n, seed=1)
     A0, B0 = _dev(torch, a), _dev(torch, b)

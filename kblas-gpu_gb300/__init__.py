@@ -174,6 +174,8 @@ def probe_lib():
             _probe = C.CDLL(PROBE_PATH)
             _probe.kblas_probe_fma.restype = C.c_float
             _probe.kblas_probe_fma.argtypes = [I, I, I, I, I, P]
+            _probe.kblas_probe_fma64_lanes.restype = C.c_float
+            _probe.kblas_probe_fma64_lanes.argtypes = [I, I, I, I, P]
     return _probe
 
 

@@ -28,6 +28,7 @@ namespace kgb {
 #ifndef KGB_SUBPHASE_BEGIN
 #define KGB_SUBPHASE_BEGIN(t)
 #define KGB_SUBPHASE_MARK(t, k)
+#define KGB_SUBPHASE_MARK1(t, k)
 #endif
 
 constexpr int PNB = 32;  // panel width
@@ -176,6 +177,28 @@ __device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T 
   __syncwarp();
 }
 
+// Warp 0: factor the diagonal block of panel p in registers; L -> panel and
+// -> Ldb (row-major copy, stride LDD); 1/L(c,c) -> rinv; *flag = failing
+// column (global, 1-based) or 0. Kept out of line: both panel
+// factorizations call it, and the ~21 KB of unrolled code then exists once.
+template <typename T, bool CHECK_INF>
+__device__ __noinline__ void warp_factor_diag(const PanelLayout &L, int p, T *Ps, T *Ldb, T *rinv,
+                                                 T tol, int *flag)
+{
+  const int lane = threadIdx.x & 31;
+  const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
+  T *Pp = Ps + L.base(p);
+  T v[32];
+#pragma unroll
+  for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
+  const int f = warp_chol_unrolled<T, CHECK_INF>(v, jb, tol, Ldb, LDD, rinv + J);
+  __syncwarp();
+  for (int c = 0; c < jb; c++)
+    if (lane >= c && lane < jb) Pp[lane + c * ld] = Ldb[lane * LDD + c];
+  if (lane == 0) *flag = f ? J + f : 0;
+  __syncwarp();
+}
+
 // ----------------------------------------------------------------------------
 // Panel Cholesky of the team's matrix. Ps: panel storage (shared or global).
 // Ld: 32 x 32 row-major scratch (shared) for the current diagonal block.
@@ -195,19 +218,9 @@ __device__ int team_potrf_panel(const Team &t, const PanelLayout &L, T *Ps, T *L
   for (int p = 0; p < L.np; p++) {
     const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
     T *Pp = Ps + L.base(p);
-    // (a) diagonal block, warp 0, lane = row: L -> Ld (row-major), then -> panel
-    if (w == 0) {
-      T v[32];
-#pragma unroll
-      for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
-      const int f = warp_chol_unrolled<T, CHECK_INF>(v, jb, tol, Ld, LDD, rinv + J);
-      __syncwarp();
-      // write L_JJ back column by column (coalesced in the panel); with INV it
-      // is replaced by the inverse later in this step
-      for (int c = 0; c < jb; c++)
-        if (lane >= c && lane < jb) Pp[lane + c * ld] = Ld[lane * LDD + c];
-      if (lane == 0) *flag = f ? J + f : 0;
-    }
+    // (a) diagonal block, warp 0, lane = row: L -> Ld (row-major), then -> the
+    // panel (with INV it is replaced by the inverse after the last step)
+    if (w == 0) warp_factor_diag<T, CHECK_INF>(L, p, Ps, Ld, rinv, tol, flag);
     t.sync();
     fail = *flag;
     if (fail) break;
@@ -350,26 +363,6 @@ __device__ __forceinline__ void panel_tile_update(const T *Pp, int ld, int jb, i
   }
 }
 
-// Warp 0: factor the diagonal block of panel p in registers; L -> panel and
-// -> Ldb (row-major copy, stride LDD); 1/L(c,c) -> rinv; *flag = failing
-// column (global, 1-based) or 0.
-template <typename T, bool CHECK_INF>
-__device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T *Ps, T *Ldb, T *rinv,
-                                                 T tol, int *flag)
-{
-  const int lane = threadIdx.x & 31;
-  const int J = p * PNB, jb = L.jb(p), ld = L.ldp(p);
-  T *Pp = Ps + L.base(p);
-  T v[32];
-#pragma unroll
-  for (int c = 0; c < 32; c++) v[c] = (c < jb && c <= lane && lane < jb) ? Pp[lane + c * ld] : T(0);
-  const int f = warp_chol_unrolled<T, CHECK_INF>(v, jb, tol, Ldb, LDD, rinv + J);
-  __syncwarp();
-  for (int c = 0; c < jb; c++)
-    if (lane >= c && lane < jb) Pp[lane + c * ld] = Ldb[lane * LDD + c];
-  if (lane == 0) *flag = f ? J + f : 0;
-  __syncwarp();
-}
 
 // The trailing update of step p by warps 1.. of a look-ahead team, FP32/FP64
 // FMAs in 4 x 4 register tiles; the next panel's diagonal block (warp 0's)
@@ -661,14 +654,18 @@ __device__ int team_potrf_panel_la(const Team &t, const PanelLayout &L, T *Ps, T
           panel_tile_update<T>(Pp, ld, jb, K - J, r4 * 4, c4 * 4, Pq, L.ldp(q), jq);
         }
         __syncwarp();
+        KGB_SUBPHASE_MARK(t, 12);
         warp_factor_diag<T, CHECK_INF>(L, q, Ps, Ld2 + (q & 1) * 32 * LDD, rinv, tol, flag);
+        KGB_SUBPHASE_MARK(t, 13);
       }
     } else if constexpr (sizeof(T) == 4) {
+      KGB_SUBPHASE_MARK1(t, 15);
       if (tc && p + 1 < L.np) {
         team_trailing_tc(t, L, p, reinterpret_cast<float *>(Ps), *tc);
       } else {
         trailing_update_ffma<T>(t, L, p, Ps);
       }
+      KGB_SUBPHASE_MARK1(t, 14);
     } else {
       trailing_update_ffma<T>(t, L, p, Ps);
     }

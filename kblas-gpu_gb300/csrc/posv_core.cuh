@@ -87,10 +87,10 @@ struct PosvCfg {
 // k = log2(sqrt(n) u32 / ((9n - 2) u64)) / -log2(rho_hat) refinement steps,
 // each one FP64 residual sweep (n^2 nr FMAs) after the first, against n^3 / 6
 // + n^2 nr for the FP64 factor and solve: a system goes straight to the FP64
-// path when rho_hat >= 1/2 or k > n / (6 nr). The refinement's own cost-model
-// exit (refine_too_slow) still catches what the estimate misses. Panel path
-// only (n > 32): below that the FP64 factorization is not the cheaper path
-// in practice (every step is latency, not FP64 work).
+// path when rho_hat >= 1/2 or k > max(n / (6 nr), 1.5). The refinement's own
+// cost-model exit (refine_too_slow) still catches what the estimate misses.
+// Panel path only (n > 32): below that the FP64 factorization is not the
+// cheaper path in practice (every step is latency, not FP64 work).
 __device__ __forceinline__ bool route_fp64(float dmin, int n, int nr, float c) {
   if (!(c > 0.f)) return false;
   if (!(dmin > 0.f)) return true;
@@ -98,7 +98,9 @@ __device__ __forceinline__ bool route_fp64(float dmin, int n, int nr, float c) {
   if (!(rho < 0.5f)) return true;
   const float l = 29.0f + 0.5f * log2f((float)n) - log2f(9.0f * n - 2.0f);
   const float k = l / -log2f(rho);
-  return k > (float)n / (6.0f * (float)nr);
+  // a system that converges in one or two steps stays on the mixed path even
+  // when many right-hand sides make the FP64 factorization cheap
+  return k > fmaxf((float)n / (6.0f * (float)nr), 1.5f);
 }
 
 __host__ __device__ __forceinline__ int pc_class(const PosvCfg &c, int n) {
@@ -642,8 +644,10 @@ __device__ __forceinline__ void item_decode(const ItemArgs &it, const PosvCfg &c
 }
 
 // Ask L2 for the lower triangles of the next item's matrices while the
-// current item is being processed (one prefetch per 128-byte line), so the
-// next item's staging loads hit L2 instead of waiting on HBM.
+// current item is being processed, so the next item's staging loads hit L2
+// instead of waiting on HBM: one TMA bulk prefetch per column (rows j..n-1,
+// contiguous), trimmed inward to 16-byte boundaries as the bulk operation
+// requires, so it never reaches outside the column's own range.
 __device__ __forceinline__ void prefetch_item(const SysArgs &sys, const ItemArgs &it,
                                               const PosvCfg &cfg, long long q) {
   int n, start, count;
@@ -655,9 +659,11 @@ __device__ __forceinline__ void prefetch_item(const SysArgs &sys, const ItemArgs
     int m, lda, ldb;
     double *A, *B;
     sys.get(sidx, m, A, lda, B, ldb);
-    const char *lo = reinterpret_cast<const char *>(A + (size_t)j + (size_t)j * lda);
-    const char *hi = reinterpret_cast<const char *>(A + (size_t)n + (size_t)j * lda);
-    for (const char *a = lo; a < hi; a += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(A + (size_t)j + (size_t)j * lda);
+    const uintptr_t hi = reinterpret_cast<uintptr_t>(A + (size_t)n + (size_t)j * lda);
+    const uintptr_t lo16 = (lo + 15) & ~(uintptr_t)15, hi16 = hi & ~(uintptr_t)15;
+    if (hi16 > lo16)
+      bulk_prefetch_l2(reinterpret_cast<const void *>(lo16), (uint32_t)(hi16 - lo16));
   }
 }
 // PATHS selects the code compiled in: bit 0 the register path (n <= 32), bit
@@ -678,6 +684,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
   // tensor-core trailing updates (mixed panel path): the CTA holds all TMEM
   // columns for the whole launch (one CTA per SM) and one mbarrier
   const bool use_tc = MIXED && (PATHS & 2) != 0 && out.tc != 0;
+  if (threadIdx.x == 0) s_abort = 0;
   if (use_tc) {
     if (threadIdx.x < 32) {
       tmem_alloc(&s_tmem, TC_TMEM_COLS);
@@ -686,12 +693,11 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
     if (threadIdx.x == 0) {
       mbar_init(&s_tcbar, 1);
       mbar_init_fence();
-      s_abort = 0;
     }
     tc_fence_before_sync();
-    __syncthreads();
-    tc_fence_after_sync();
   }
+  __syncthreads();
+  if (use_tc) tc_fence_after_sync();
   TcCtx tcx{use_tc ? s_tmem : 0u, &s_tcbar, nullptr, &s_abort, out.status, 0u};
   long long first = 0, nitems;
   if (it.uniform) {
@@ -708,7 +714,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
   for (;;) {
     __syncthreads();
     const long long q = s_item;
-    const bool stop = use_tc && s_abort != 0;
+    const bool stop = s_abort != 0;
     __syncthreads();
     if (q >= nitems || stop) break;
     // claim the next item now and warm L2 with its matrices

@@ -5,7 +5,8 @@
 // Xpotrs_batch.cu:87-165 and Xposv_batch.cu:92-178 (same names, arguments,
 // flag support and return codes). Unlike the reference (host recursion over
 // TRSM + SYRK + cuBLAS GEMM, 4 launches at n = 32 and one HBM pass per level),
-// every call is ONE kernel launch: the team kernel for n <= 32 and, above,
+// every call is ONE kernel launch: for n <= 32 the team kernel (POTRS of real
+// types: the register kernel, chol_reg.cuh) and, above,
 // the persistent panel kernel (double precision, when the workspace the
 // wsqueries request is allocated) or the blocked panel kernel (see
 // chol_kernels.cuh).
@@ -15,6 +16,7 @@
 #include <cuComplex.h>
 
 #include "chol_kernels.cuh"
+#include "chol_reg.cuh"
 #include "kblas_internal.h"
 #include "launch_util.h"
 #include "posv_launch.h"
@@ -47,6 +49,22 @@ static int launch_team(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, in
   return KBLAS_Success;
 }
 
+// POTRS, n <= 32, real types: one factor per W-lane segment, rows in registers.
+template <typename T, int W, class AccA, class AccB>
+static int launch_potrs_reg(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
+                            long long batch) {
+  constexpr int NT = 128;
+  constexpr int SPB = NT / W;  // systems per CTA
+  const size_t smem = (size_t)SPB * reg_square_elems<T, W>() * sizeof(T);
+  auto kern = potrs_reg_kernel<T, W, NT, AccA, AccB>;
+  int st = set_smem(kern, smem);
+  if (st != KBLAS_Success) return st;
+  long long grid = (batch + SPB - 1) / SPB;
+  kern<<<(unsigned)grid, NT, smem, h->stream>>>(n, m, A, lda, B, ldb, batch);
+  KGB_LAUNCH_CHECK("potrs_reg_kernel");
+  return KBLAS_Success;
+}
+
 template <typename T, int NB, int MODE, class AccA, class AccB>
 static int launch_blocked_nb(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
                              long long batch, int *info, size_t smem, int rc) {
@@ -63,6 +81,18 @@ static int launch_blocked_nb(KBlasHandle *h, int n, int m, AccA A, int lda, AccB
 template <typename T, int MODE, class AccA, class AccB>
 static int launch_chol(KBlasHandle *h, int n, int m, AccA A, int lda, AccB B, int ldb,
                        long long batch, int *info) {
+  // POTRS of order <= 32 runs on the register kernel (real types). POTRF and
+  // POSV stay on the team kernel: the register factorization keeps a row per
+  // lane, so at column c only the rows below c do useful work, and on this
+  // part an FP64 instruction costs its issue slot whether or not its lane is
+  // predicated off -- it measured slower (n = 32, 10,000 matrices: POTRF 438
+  // vs 310 us, POSV 605 vs 369 us; POTRS 105 vs 122 us).
+  if constexpr (MODE == MODE_POTRS &&
+                (std::is_same<T, double>::value || std::is_same<T, float>::value)) {
+    if (n <= 8) return launch_potrs_reg<T, 8>(h, n, m, A, lda, B, ldb, batch);
+    if (n <= 16) return launch_potrs_reg<T, 16>(h, n, m, A, lda, B, ldb, batch);
+    if (n <= 32) return launch_potrs_reg<T, 32>(h, n, m, A, lda, B, ldb, batch);
+  }
   if (n <= 32) {
     switch (team_size_for(n, std::is_same<T, double>::value)) {
       case 2: return launch_team<T, 2, MODE>(h, n, m, A, lda, B, ldb, batch, info);

@@ -22,6 +22,26 @@ __global__ void fma_chain_kernel(T *out, int iters, T a, T b) {
   if (s == T(1234.5)) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The same chains run only by lanes < active of each warp (the others skip
+// them under a branch): the kernel time shows whether the FP64 pipe spends
+// an issue slot on the lanes that do not take part.
+template <typename T, int ILP>
+__global__ void fma_chain_lanes_kernel(T *out, int iters, int active, T a, T b) {
+  T x[ILP];
+#pragma unroll
+  for (int i = 0; i < ILP; i++) x[i] = T(threadIdx.x + i) * T(1e-3);
+  if ((int)(threadIdx.x & 31) < active) {
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+      for (int i = 0; i < ILP; i++) x[i] = x[i] * a + b;
+    }
+  }
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < ILP; i++) s += x[i];
+  if (s == T(1234.5)) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 template <typename T, int ILP>
 static float run_chain(int blocks, int threads, int iters, void *scratch) {
   cudaEvent_t e0, e1;
@@ -60,6 +80,25 @@ float kblas_probe_fma(int prec, int blocks, int threads, int iters, int ilp, voi
     }
   }
   return -1.f;
+}
+
+// FP64 chains (ILP 4) run by `active` lanes of every warp; returns the kernel
+// time in ms (one warm-up launch, one timed), or -1.
+float kblas_probe_fma64_lanes(int blocks, int threads, int iters, int active, void *scratch) {
+  if (active < 1 || active > 32) return -1.f;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fma_chain_lanes_kernel<double, 4><<<blocks, threads>>>((double *)scratch, iters, active, 0.999999, 1e-7);
+  cudaEventRecord(e0);
+  fma_chain_lanes_kernel<double, 4><<<blocks, threads>>>((double *)scratch, iters, active, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
 }
 
 }  // extern "C"

@@ -23,7 +23,6 @@ namespace kgb {
 
 constexpr uint32_t TC_LBO = 128;   // bytes between core matrices adjacent along K
 constexpr uint32_t TC_SBO = 512;   // bytes between 8-row groups (K = 32 per row)
-constexpr uint32_t TC_ROWB = 64;   // bytes per 8-row group row-stride unit: 32 BF16
 constexpr int TC_TMEM_COLS = 512;  // TMEM columns a CTA takes (all of them)
 constexpr long long TC_WAIT_LIMIT = 1ll << 22;  // polls before a wait gives up
 
@@ -85,6 +84,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     if (i > 64) __nanosleep(32);
   }
   return false;
+}
+
+// ---- bulk prefetch (TMA unit, no tensor map) --------------------------------
+// Ask the TMA unit to bring [src, src + bytes) into L2 (a hint: nothing is
+// waited for). src 16-byte aligned, bytes a positive multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 // ---- descriptors ------------------------------------------------------------

@@ -25,8 +25,18 @@ static __device__ unsigned long long kgb_phase_acc[32];
   } while (0)
 #define KGB_PHASE_BEGIN(t) long long kgb_pt_ = clock64()
 #define KGB_PHASE_MARK(t, k) KGB_PHASE_TICK_(t, k, kgb_pt_)
-#define KGB_SUBPHASE_BEGIN(t) long long kgb_spt_ = clock64()
+#define KGB_SUBPHASE_BEGIN(t) long long kgb_spt_ = clock64(), kgb_spt1_ = kgb_spt_
 #define KGB_SUBPHASE_MARK(t, k) KGB_PHASE_TICK_(t, k, kgb_spt_)
+// the same, counted by the team's thread 32 (the first lane of warp 1)
+#define KGB_SUBPHASE_MARK1(t, k)                                                         \
+  do {                                                                                   \
+    const long long now_ = clock64();                                                    \
+    if ((t).tid == 32) {                                                                 \
+      atomicAdd(&kgb_phase_acc[(k)], (unsigned long long)(now_ - kgb_spt1_));            \
+      atomicAdd(&kgb_phase_acc[16 + (k)], 1ull);                                         \
+    }                                                                                    \
+    kgb_spt1_ = now_;                                                                    \
+  } while (0)
 
 typedef int (*kgb_phase_fn)(unsigned long long *, int);
 extern "C" __attribute__((weak)) kgb_phase_fn kgb_phase_fns[64] = {0};

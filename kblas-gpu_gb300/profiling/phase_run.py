@@ -9,7 +9,9 @@ factor (FP32 panel Cholesky + diagonal-block inverses), solve0 (first FP32
 solve, per sweep of up to 4 right-hand sides), residual (FP64 r = b - A x,
 per sweep), solve_corr (convergence test + FP32 correction solve, per step),
 tail (write-back). Sub-phases of the factorization (chol_panel.cuh,
-team_potrf_panel_la): f:diag0, f:rows_trsm, f:trailing, f:invert.
+team_potrf_panel_la): f:diag0, f:rows_trsm, f:trailing, f:invert; inside
+f:trailing, warp 0's look-ahead (update and factor of the next diagonal
+block) and, timed by warp 1, the trailing update of the other warps.
 
 Run on the GPU:  python kblas-gpu_gb300/profiling/phase_build.py &&
                  python kblas-gpu_gb300/profiling/phase_run.py [batch n nrhs [sqexp|spd]]
@@ -28,7 +30,9 @@ import torch
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 NAMES = {0: "stage", 1: "factor", 2: "solve0", 3: "residual", 4: "solve_corr", 5: "tail",
-         8: "f:diag0", 9: "f:rows_trsm", 10: "f:trailing", 11: "f:invert"}
+         8: "f:diag0", 9: "f:rows_trsm", 10: "f:trailing", 11: "f:invert",
+         12: "f:w0_next_block_update", 13: "f:w0_next_block_factor",
+         14: "f:w1_trailing_update", 15: "f:w1_before_update"}
 
 
 def _load(name, path, pkg=False):

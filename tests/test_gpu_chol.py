@@ -145,6 +145,51 @@ def test_posv_and_potrs(gpu, handle, wl, orc, dt, n, m, form):
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["d", "s"])
+@pytest.mark.parametrize("n", [1, 3, 7, 8, 9, 15, 16, 17, 30, 31, 32])
+@pytest.mark.parametrize("pad", [0, 4])
+def test_register_kernel_vector_path(gpu, handle, wl, orc, dt, n, pad):
+    """n <= 32 with 16-byte aligned matrices and lda a multiple of 16 bytes:
+    POTRS runs on the register kernel, which loads the factor in 128-bit
+    chunks; POTRF and POSV (team kernel) leave the strict upper triangle and
+    the padding rows untouched, and all three agree with the oracle."""
+    batch, m = 37, 3
+    lda = -(-n // 4) * 4 + pad  # 16-byte multiple for both precisions
+    a = make_batch(wl, batch, n, lda, dt, seed=300 + n)
+    ref = a.copy()
+    info_ref = orc.potrf_batch(ref, n)
+    pfx = "D" if dt == np.float64 else "S"
+    da = to_dev(gpu, a)
+    assert da.data_ptr() % 16 == 0
+    dinfo = gpu.full((batch,), -99, dtype=gpu.int32, device="cuda")
+    assert handle.call(f"kblas{pfx}potrf_batch_strided", "L", n, da.data_ptr(), lda, n * lda, batch,
+                       dinfo.data_ptr()) == 1
+    gpu.cuda.synchronize()
+    out = da.cpu().numpy()
+    assert np.array_equal(dinfo.cpu().numpy(), info_ref)
+    check_untouched(a, out, n)
+    tol = 10 * max(n, 2) * eps(dt)
+    rd = max(np.abs(np.tril(out[b, :n, :n].T) - np.tril(ref[b, :n, :n].T)).max()
+             / np.abs(np.tril(ref[b, :n, :n].T)).max() for b in range(batch))
+    assert rd <= tol, rd
+    # POSV and POTRS (right-hand sides as rows of B, ldb = m)
+    bmat = wl.rhs_rows(batch, m, n, seed=n + 5, dtype=np.float64).astype(dt)
+    da, db = to_dev(gpu, a), to_dev(gpu, bmat)
+    assert handle.call(f"kblas{pfx}posv_batch_strided", "R", "L", m, n, da.data_ptr(), lda,
+                       n * lda, db.data_ptr(), m, n * m, batch, dinfo.data_ptr()) == 1
+    gpu.cuda.synchronize()
+    X = db.cpu().numpy()
+    check_untouched(a, da.cpu().numpy(), n)
+    eta = orc.backward_error_r(a.astype(np.float64), X.astype(np.float64),
+                               bmat.astype(np.float64), m, n)
+    assert eta.max() <= 10 * n * eps(dt), eta.max()
+    db2 = to_dev(gpu, bmat)
+    assert handle.call(f"kblas{pfx}potrs_batch_strided", "R", "L", m, n, da.data_ptr(), lda,
+                       n * lda, db2.data_ptr(), m, n * m, batch) == 1
+    gpu.cuda.synchronize()
+    assert np.abs(db2.cpu().numpy() - X).max() <= 64 * n * eps(dt) * max(1.0, np.abs(X).max())
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32], ids=["d", "s"])
 def test_info_codes_match_lapack_golden(gpu, handle, golden, dt):
     """Non-SPD matrices with a known failing leading minor (LAPACK golden
     vectors): identical info, B untouched by POSV for the failed systems."""

@@ -127,8 +127,14 @@ def test_mixed_panel_path_several_rhs_covariance(gpu, handle, kb, wl, orc, n, m)
     batch = 6
     a = wl.sqexp_cov(batch, n, seed=n + m)
     b = wl.rhs_rows(batch, m, n, seed=5 * m + 1)
-    A, X, info, it = run_uniform_mixed(gpu, kb, handle, a, b, m, n,
-                                       form="strided" if m % 2 else "array")
+    # the refinement sweeps are what this test exercises: no conditioning
+    # routing to FP64 (with it, most of these systems take the FP64 path)
+    assert kb.lib().kblasSetPosvRouting(0.0) == 1
+    try:
+        A, X, info, it = run_uniform_mixed(gpu, kb, handle, a, b, m, n,
+                                           form="strided" if m % 2 else "array")
+    finally:
+        assert kb.lib().kblasSetPosvRouting(-1.0) == 1
     assert (info == 0).all()
     eta = orc.backward_error_r(a, X, b, m, n)
     assert eta.max() <= 10 * n * EPS64, eta.max()
