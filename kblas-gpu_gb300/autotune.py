@@ -10,6 +10,13 @@ on a batch whose orders are log-uniform over that class, and keeps the fastest.
 The chosen table is applied at run time through kblasSetPosvTuning while it
 is measured, and written out as a header to be compiled in.
 
+It also tunes the mixed path's conditioning-routing constant (the c of
+route_fp64 in csrc/posv_core.cuh, set through kblasSetPosvRouting): on a
+uniform batch of n = 64 systems with 4 right-hand sides and condition numbers
+log-uniform in [1e2, 1e8] it times the mixed POSV for each candidate c (0 =
+no routing) and keeps the fastest; every candidate's results must meet the
+backward-error bar (checked on the device: info 0 for all systems).
+
 Run on the GPU:  python kblas-gpu_gb300/autotune.py --out <path>/tuning_table.h
 """
 from __future__ import annotations
@@ -126,6 +133,72 @@ def time_call(torch, kb, h, cb, mixed, reps):
     return float(np.median(times))
 
 
+ROUTE_CANDIDATES = [0.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0]
+
+
+class CondBatch:
+    """Uniform strided batch of n = 64 SPD systems A = Q diag(l) Q^T (Q from
+    the QR of a Gaussian matrix, l geometric with cond log-uniform in
+    [1e2, 1e8]) and 4 right-hand sides."""
+
+    def __init__(self, torch, batch=20_000, n=64, m=4, seed=7):
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(seed)
+        q, _ = torch.linalg.qr(torch.randn((batch, n, n), generator=gen, dtype=torch.float64,
+                                           device="cuda"))
+        lc = torch.rand(batch, generator=gen, dtype=torch.float64, device="cuda") * 6 + 2
+        t = torch.linspace(0, 1, n, dtype=torch.float64, device="cuda")
+        lam = torch.pow(10.0, -lc[:, None] * t[None, :])
+        a = (q * lam[:, None, :]) @ q.transpose(1, 2)
+        self.A0 = (0.5 * (a + a.transpose(1, 2))).contiguous()
+        self.B0 = torch.randn((batch, n, m), generator=gen, dtype=torch.float64, device="cuda")
+        self.A, self.B = self.A0.clone(), self.B0.clone()
+        self.info = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        self.iter = torch.zeros(batch, dtype=torch.int32, device="cuda")
+        self.batch, self.n, self.m = batch, n, m
+
+
+def time_route(torch, kb, h, cb, reps):
+    stream = torch.cuda.current_stream()
+    times = []
+    for r in range(reps + 2):
+        cb.A.copy_(cb.A0)
+        cb.B.copy_(cb.B0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = h.call("kblasDposv_batch_mixed_strided", "R", "L", cb.m, cb.n, cb.A.data_ptr(), cb.n,
+                    cb.n * cb.n, cb.B.data_ptr(), cb.m, cb.n * cb.m, cb.batch,
+                    cb.info.data_ptr(), cb.iter.data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        if st != 1:
+            raise RuntimeError(f"kblasDposv_batch_mixed_strided returned {st}")
+        if r >= 2:
+            times.append(e0.elapsed_time(e1))
+    if int((cb.info != 0).sum()) != 0:
+        raise RuntimeError("routing batch produced non-zero info")
+    return float(np.median(times))
+
+
+def tune_route(torch, kb, reps=5, log=print):
+    """Returns {"route_c": best, "ms": {c: ms}}."""
+    h = kb.Handle(stream=torch.cuda.current_stream().cuda_stream)
+    cb = CondBatch(torch)
+    res = {}
+    try:
+        kb.lib().kblas_posv_batch_mixed_wsquery(h.ptr, b"R", cb.m, cb.n, cb.batch)
+        kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
+        for c in ROUTE_CANDIDATES:
+            kb.check(kb.lib().kblasSetPosvRouting(c), "kblasSetPosvRouting")
+            res[c] = time_route(torch, kb, h, cb, reps)
+            log(f"route c {c:g}: {res[c]:.3f} ms")
+    finally:
+        kb.lib().kblasSetPosvRouting(-1.0)
+        torch.cuda.synchronize()
+        h.close()
+    return {"route_c": min(res, key=res.get), "ms": res}
+
+
 def set_table(kb, mixed, ts, spi):
     C = __import__("ctypes")
     arr = lambda v: (C.c_int * NCLS)(*v)
@@ -185,6 +258,13 @@ def header_text(result, device_name):
         "",
         "// {nmax}, {team size}, {systems per item}",
     ]
+    route = result.get("route")
+    if route:
+        lines.append("// conditioning routing constant of the mixed path (route_fp64): the")
+        lines.append("// fastest mixed POSV on n = 64, 4 RHS, cond 1e2..1e8 (ms per call: "
+                     + ", ".join(f"c {k:g}: {v:.3f}" for k, v in route["ms"].items()) + ")")
+        lines.append(f"#define KGB_TUNE_ROUTE_C {route['route_c']:g}f")
+        lines.append("")
     for form, tag in (("mixed", "MIXED"), ("plain", "PLAIN")):
         r = result[form]
         lines.append(f"#define KGB_TUNE_{tag}_NMAX {{{', '.join(map(str, NMAX))}}}")
@@ -209,6 +289,7 @@ def main():
     kb = load_pkg()
     kb.lib()
     result = tune(torch, kb, reps=args.reps)
+    result["route"] = tune_route(torch, kb, reps=args.reps)
     text = header_text(result, torch.cuda.get_device_name(0))
     with open(args.out, "w") as f:
         f.write(text)

@@ -586,6 +586,13 @@ static __device__ bool team_trailing_tc(const Team &t, const PanelLayout &L, int
     }
     tc_fence_before_sync();
     asm volatile("bar.sync 15, %0;" ::"r"(unt) : "memory");
+    if (*tc.abort) {
+      // a wait ran out (the flag is read after the barrier, so every thread
+      // decides alike): no more MMAs; wait once more, bounded, for the ones
+      // in flight before the CTA stops and frees its TMEM
+      mbar_wait_bounded(tc.bar, (tc.round - 1u) & 1u);
+      return false;
+    }
     c_first = c_end;
   }
   return ok;
