@@ -263,7 +263,7 @@ def header_text(result, device_name):
         lines.append("// conditioning routing constant of the mixed path (route_fp64): the")
         lines.append("// fastest mixed POSV on n = 64, 4 RHS, cond 1e2..1e8 (ms per call: "
                      + ", ".join(f"c {k:g}: {v:.3f}" for k, v in route["ms"].items()) + ")")
-        lines.append(f"#define KGB_TUNE_ROUTE_C {route['route_c']:g}f")
+        lines.append(f"#define KGB_TUNE_ROUTE_C {float(route['route_c']):.1f}f")
         lines.append("")
     for form, tag in (("mixed", "MIXED"), ("plain", "PLAIN")):
         r = result[form]

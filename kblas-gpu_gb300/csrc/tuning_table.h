@@ -6,33 +6,32 @@
 #pragma once
 
 // {nmax}, {team size}, {systems per item}
+// conditioning routing constant of the mixed path (route_fp64): the
+// fastest mixed POSV on n = 64, 4 RHS, cond 1e2..1e8 (ms per call: c 0: 8.370, c 4: 6.742, c 8: 6.741, c 16: 6.626, c 32: 6.501, c 64: 6.569, c 128: 6.681)
+#define KGB_TUNE_ROUTE_C 32.0f
+
 #define KGB_TUNE_MIXED_NMAX {8, 16, 32, 64, 96, 128, 176, 1024}
 #define KGB_TUNE_MIXED_TS {8, 16, 32, 32, 64, 32, 128, 256}
 #define KGB_TUNE_MIXED_SPI {32, 16, 8, 8, 4, 8, 2, 1}
-
-// conditioning routing constant of the mixed path (route_fp64); measured
-// on the n = 64, 4-RHS, cond 1e2..1e8 batch: c = 0 / 8 / 32 -> mixed at
-// 0.72 / 0.89 / 0.92 of the FP64 form; no effect on well-conditioned batches
-#define KGB_TUNE_ROUTE_C 32.0f
 
 #define KGB_TUNE_PLAIN_NMAX {8, 16, 32, 64, 96, 128, 176, 1024}
 #define KGB_TUNE_PLAIN_TS {8, 16, 32, 32, 32, 32, 64, 64}
 #define KGB_TUNE_PLAIN_SPI {32, 16, 8, 8, 8, 8, 4, 4}
 
 // measured ms per call, class: {team size: ms}
-//   mixed class 0: 8: 1.109, 16: 2.432, 32: 6.469
-//   mixed class 1: 16: 2.664, 32: 6.786
-//   mixed class 2: 32: 7.768
-//   mixed class 3: 32: 6.516, 64: 10.113, 128: 18.904
-//   mixed class 4: 32: 6.401, 64: 6.303, 128: 9.975, 256: 18.859
-//   mixed class 5: 32: 6.112, 64: 6.398, 128: 6.692, 256: 11.846
-//   mixed class 6: 64: 7.724, 128: 5.941, 256: 8.501
-//   mixed class 7: 64: 8.615, 128: 8.101, 256: 6.414
-//   plain class 0: 8: 0.620, 16: 1.064, 32: 2.425
-//   plain class 1: 16: 2.391, 32: 6.629
-//   plain class 2: 32: 12.191
-//   plain class 3: 32: 13.101, 64: 17.302, 128: 32.088
-//   plain class 4: 32: 13.128, 64: 15.527, 128: 23.195, 256: 43.106
-//   plain class 5: 32: 14.885, 64: 15.962, 128: 20.609, 256: 34.544
-//   plain class 6: 64: 17.927, 128: 21.214, 256: 30.100
-//   plain class 7: 64: 20.508, 128: 22.974, 256: 28.593
+//   mixed class 0: 8: 1.179, 16: 2.547, 32: 6.643
+//   mixed class 1: 16: 2.766, 32: 6.868
+//   mixed class 2: 32: 7.839
+//   mixed class 3: 32: 6.664, 64: 10.222, 128: 19.111
+//   mixed class 4: 32: 6.523, 64: 6.368, 128: 10.148, 256: 19.466
+//   mixed class 5: 32: 6.148, 64: 6.458, 128: 6.825, 256: 12.230
+//   mixed class 6: 64: 7.771, 128: 6.020, 256: 8.805
+//   mixed class 7: 64: 8.633, 128: 8.100, 256: 6.600
+//   plain class 0: 8: 0.637, 16: 1.086, 32: 2.462
+//   plain class 1: 16: 2.444, 32: 6.725
+//   plain class 2: 32: 12.273
+//   plain class 3: 32: 13.197, 64: 17.274, 128: 32.045
+//   plain class 4: 32: 13.121, 64: 15.425, 128: 23.138, 256: 42.936
+//   plain class 5: 32: 14.882, 64: 15.877, 128: 20.607, 256: 34.454
+//   plain class 6: 64: 17.888, 128: 21.046, 256: 30.013
+//   plain class 7: 64: 20.475, 128: 22.847, 256: 28.391
