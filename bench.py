@@ -469,7 +469,7 @@ def cfg_potrf_potrs_n32(c, cpu_seconds=3.0):
     REPS back-to-back POTRF + POTRS pairs, each on its own copy of the batch
     (REPS x 82 MB, larger than L2), inside one CUDA event pair."""
     torch, kb, h, orc, wl = c.torch, c.kb, c.h, c.orc, c.wl
-    batch, n, reps = 10_000, 32, 100
+    batch, n, reps = 10_000, 32, c.args.reps
     a = wl.spd_shifted(batch, n, seed=0)
     b = wl.rhs_rows(batch, 1, n, seed=0)
     A0, B0 = _dev(torch, a), _dev(torch, b)
@@ -955,6 +955,9 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--batch", type=int, default=100_000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--reps", type=int, default=100,
+                    help="potrf_potrs_n32: POTRF + POTRS pairs per step, each on its own copy "
+                         "of the 82 MB batch (fewer for profiler captures)")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the other configurations after the variable-size headline")
     ap.add_argument("--workload", default="vbatch",
