@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "batched POSV solves/s at backward err ≤10·n·eps64: mixed-prec vs plain FP64"
 EPS64 = 2.0 ** -53
 E2E_CHUNKS = 16
+LINK_PROBE_REPS = 5  # plain host->device copies of the matrix pool after the e2e steps
 WORKLOAD = ("variable-size DPOSV: 100000 SPD systems, n log-uniform integer 8..256, "
             "A = G G^T + n I, 1 RHS, pointer arrays, 1% indefinite (one eigenvalue flipped)")
 
@@ -1076,6 +1077,17 @@ def main():
     t_e2e = timed_steps(torch, e2e_step, lambda: None, args.steps, args.warmup, stream)
     torch.cuda.synchronize()
     h2d_ms = [a.elapsed_time(b) for a, b in h2d_events[-args.steps:]]
+    # the host link alone: the same host->device copy of the matrix pool with
+    # no solve running, repeated; its spread is the link's, not the solver's
+    link_ms = []
+    for _ in range(LINK_PROBE_REPS):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(copy_stream):
+            e0.record(copy_stream)
+            w.A.copy_(hA, non_blocking=True)
+            e1.record(copy_stream)
+        e1.synchronize()
+        link_ms.append(e0.elapsed_time(e1))
     e2e_info = np.zeros(w.batch, dtype=np.int32)
     for c, (lo, hi) in zip(chunks, [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]):
         e2e_info[order[lo:hi]] = c["hinfo"].numpy()
@@ -1137,8 +1149,8 @@ def main():
                      "note": "algorithmic bytes over the event-timed call. The persistent "
                              "mixed kernel binds on neither HBM nor tensor cores: it is "
                              "latency-bound (team barriers, dependent FMA chains, L2 round "
-                             "trips); ncu: DRAM throughput 1.6%, FP64 pipe 23%, FP32 8% "
-                             "(profiles/posv_vbatch_mixed_n8-256.txt). The FP64 form's "
+                             "trips); ncu: DRAM throughput 1.7%, FP64 pipe 19%, FP32 7%, "
+                             "tensor 0.6% (profiles/posv_vbatch_mixed_n8-256.txt). The FP64 form's "
                              "fraction of the FP64 pipe is in fp64_pipe"},
         "fp64_pipe": {"peak_tflops_measured_live": fp64_peak, "probe": fp64_rec["probe"],
                       "refinement_fp64_tflops": fp64_flops_refine / (ms_mixed * 1e-3) / 1e12,
@@ -1152,6 +1164,10 @@ def main():
                 "valid": e2e_valid,
                 "per_step_ms": [round(x, 3) for x in t_e2e],
                 "per_step_h2d_copy_ms": [round(x, 3) for x in h2d_ms],
+                "host_link_probe_ms": [round(x, 3) for x in link_ms],
+                "host_link_probe": "the same host->device copy of the matrix pool (pinned, "
+                                   "%.2f GB) with no solve running, %d times after the e2e steps"
+                                   % (w.pool_elems * 8 / 1e9, LINK_PROBE_REPS),
                 "pipeline": f"{len(chunks)} pieces: host->device copy of piece k+1 overlaps "
                             f"the solve of piece k (copy stream + handle stream)",
                 "vs_resident_run": e2e_check},

@@ -179,10 +179,11 @@ __device__ __forceinline__ void warp_invert_diag(T *Pp, int ld, int jb, const T 
 
 // Warp 0: factor the diagonal block of panel p in registers; L -> panel and
 // -> Ldb (row-major copy, stride LDD); 1/L(c,c) -> rinv; *flag = failing
-// column (global, 1-based) or 0. Kept out of line: both panel
-// factorizations call it, and the ~21 KB of unrolled code then exists once.
+// column (global, 1-based) or 0. Inlined: as an out-of-line call (one copy
+// of the ~21 KB of unrolled code for both panel factorizations) the mixed
+// variable-size POSV measured ~1% slower.
 template <typename T, bool CHECK_INF>
-__device__ __noinline__ void warp_factor_diag(const PanelLayout &L, int p, T *Ps, T *Ldb, T *rinv,
+__device__ __forceinline__ void warp_factor_diag(const PanelLayout &L, int p, T *Ps, T *Ldb, T *rinv,
                                                  T tol, int *flag)
 {
   const int lane = threadIdx.x & 31;
@@ -1068,6 +1069,81 @@ static __device__ void team_residual_owner(const Team &t, int n, const double *_
     double s = 0.0;
     for (int q = 0; q < nw; q++) s += rowsum[(size_t)q * n + i];
     r[i] = b[(size_t)i * incb] - s;
+  }
+  t.sync();
+}
+
+// The same residual for NR = 2..4 right-hand sides in one sweep over A: each
+// element of A is loaded once and applied to every right-hand side, so a
+// refinement step reads A once per group of right-hand sides rather than once
+// per right-hand side (at n = 512 the systems in flight hold more of A than
+// L2 does, and every extra sweep goes back to HBM). x, r: NR vectors of n
+// (stride n); right-hand side q, element i at b[q + i * ldb].
+// The tile ranges are split over nwr = min(nw, nb) warps, so that a range
+// holds at least nb tiles and a row block is shared by at most two warps;
+// each warp adds its partial rows into r (zeroed first) with shared-memory
+// atomics. Two addends onto zero give the same sum in either order, so the
+// result does not depend on which warp comes first.
+template <int NR>
+static __device__ void team_residual_multi(const Team &t, int n, const double *__restrict__ A,
+                                           int lda, const double *__restrict__ b, int ldb,
+                                           const double *x, double *r)
+{
+  const int lane = t.lane(), w = t.warp(), nw = t.nwarps();
+  const int nb = (n + 31) >> 5;
+  const int nwr = min(nw, nb);
+  const int units = nb * nb;
+  for (int i = t.tid; i < NR * n; i += t.nt) r[i] = 0.0;
+  t.sync();
+  if (w < nwr) {
+    const int u0 = (int)((long long)units * w / nwr), u1 = (int)((long long)units * (w + 1) / nwr);
+    int u = u0;
+    while (u < u1) {
+      const int I = u / nb;
+      const int uend = min(u1, (I + 1) * nb);
+      const int row = I * 32 + lane;  // output row of this lane
+      const bool rin = row < n;
+      double s[NR];
+#pragma unroll
+      for (int q = 0; q < NR; q++) s[q] = 0.0;
+      for (; u < uend; u++) {
+        const int Tb = u - I * nb;  // tile column (Tb <= I) or tile row (Tb > I)
+        const int c0 = Tb * 32;
+        const double *xt = x + c0;
+        const int cw = min(32, n - c0);
+#pragma unroll
+        for (int h = 0; h < 32; h += 16) {
+          double a[16];
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int c = h + j, col = c0 + c;
+            const bool ok = rin && c < cw;
+            size_t off;
+            if (Tb < I || (Tb == I && c <= lane)) off = (size_t)row + (size_t)col * lda;  // a(row, col)
+            else off = (size_t)col + (size_t)row * lda;  // a(col, row), the mirrored lower part
+            a[j] = ok ? A[off] : 0.0;
+          }
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const bool xin = h + j < cw;  // x past n is not this vector's (0 * NaN)
+#pragma unroll
+            for (int q = 0; q < NR; q++) {
+              const double xv = xin ? xt[(size_t)q * n + h + j] : 0.0;
+              s[q] = fma(a[j], xv, s[q]);
+            }
+          }
+        }
+      }
+      if (rin) {
+#pragma unroll
+        for (int q = 0; q < NR; q++) atomicAdd(&r[(size_t)q * n + row], s[q]);
+      }
+    }
+  }
+  t.sync();
+  for (int i = t.tid; i < n; i += t.nt) {
+#pragma unroll
+    for (int q = 0; q < NR; q++) r[(size_t)q * n + i] = b[(size_t)q + (size_t)i * ldb] - r[(size_t)q * n + i];
   }
   t.sync();
 }

@@ -41,6 +41,11 @@ namespace kgb {
 constexpr int PC_NT = 256;     // threads per persistent CTA
 constexpr int PC_NCLS = 8;     // size classes (KBLAS_POSV_TUNING_CLASSES)
 constexpr int PC_MR = 4;       // right-hand sides per residual sweep (panel path)
+// The mixed panel path runs its trailing updates on the tensor cores when a
+// launch holds orders above this: at n = 512 (8 RHS) that measured +5.6%, on
+// the n <= 256 distribution the kernel without tensor-core code was 1.5%
+// faster (at n <= 256 a step's update is too small to pay for the staging).
+constexpr int PC_TC_NMIN = 256;
 constexpr int PC_ITMAX = 12;   // refinement step cap
 constexpr double PC_EPS64 = 1.1102230246251565e-16;  // 2^-53, FP64 unit roundoff
 
@@ -555,16 +560,27 @@ static __device__ void panel_mixed_posv(const Team &t, int n, int m, double *A, 
     bool converged = false;
     int step = 0;
     for (;;) {
-      for (int q = 0; q < nr; q++) {
-        float *rowabs = (anorm < 0.0 && q == 0) ? ys : nullptr;  // ys is free here
+      // the first residual of the call also sums the rows of |A| (right-hand
+      // side 0 alone); the others go 2..4 at a time through one sweep of A
+      int q = 0;
+      if (anorm < 0.0 || nr == 1) {
+        float *rowabs = (anorm < 0.0) ? ys : nullptr;  // ys is free here
         if (rowabs)
           for (int i = t.tid; i < n; i += t.nt) rowabs[i] = 0.f;
-        team_residual_owner(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n, colsum, rowabs);
+        team_residual_owner(t, n, A, lda, B + r0, ldb, x, r, colsum, rowabs);
         if (rowabs) {
           float an_local = 0.f;
           for (int i = t.tid; i < n; i += t.nt) an_local = fmaxf(an_local, rowabs[i]);
           anorm = (double)team_max<float>(t, an_local, reinterpret_cast<float *>(red));
         }
+        q = 1;
+      }
+      switch (nr - q) {
+        case 1: team_residual_owner(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n, colsum, nullptr); break;
+        case 2: team_residual_multi<2>(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n); break;
+        case 3: team_residual_multi<3>(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n); break;
+        case 4: team_residual_multi<4>(t, n, A, lda, B + (r0 + q), ldb, x + q * n, r + q * n); break;
+        default: break;
       }
       KGB_PHASE_MARK(t, 3);
       double eta = 0.0;
@@ -667,7 +683,9 @@ __device__ __forceinline__ void prefetch_item(const SysArgs &sys, const ItemArgs
   }
 }
 // PATHS selects the code compiled in: bit 0 the register path (n <= 32), bit
-// 1 the panel path (n > 32). A kernel holding one path only gets that path's
+// 1 the panel path (n > 32), bit 2 the tensor-core trailing update of the
+// mixed panel path (a kernel without it carries none of its code, which
+// measured 1.5% faster on batches whose orders stay at or below PC_TC_NMIN). A kernel holding one path only gets that path's
 // register allocation (each path alone fits the register file; together they
 // spill), so the binned launcher runs the two paths as two launches over the
 // two item ranges: [0, *split_p) panel items, [*split_p, *nitems_p) register
@@ -683,7 +701,7 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
   __shared__ int s_abort;
   // tensor-core trailing updates (mixed panel path): the CTA holds all TMEM
   // columns for the whole launch (one CTA per SM) and one mbarrier
-  const bool use_tc = MIXED && (PATHS & 2) != 0 && out.tc != 0;
+  const bool use_tc = MIXED && (PATHS & 6) == 6 && out.tc != 0;
   if (threadIdx.x == 0) s_abort = 0;
   if (use_tc) {
     if (threadIdx.x < 32) {
@@ -705,8 +723,8 @@ posv_persistent_kernel(SysArgs sys, ItemArgs it, OutArgs out, PosvCfg cfg, int s
     nitems = (it.batch + spi - 1) / spi;
   } else {
     nitems = *it.nitems_p;
-    if (PATHS == 2) nitems = *it.split_p;
-    if (PATHS == 1) first = *it.split_p;
+    if ((PATHS & 3) == 2) nitems = *it.split_p;
+    if ((PATHS & 3) == 1) first = *it.split_p;
   }
   char *slot = out.scratch ? out.scratch + (size_t)blockIdx.x * out.slot_bytes : nullptr;
 

@@ -23,11 +23,13 @@ struct PosvPlan {
   int tc = 0;             // mixed panel path: tensor-core trailing updates for whole-CTA teams
 };
 
-// Tensor-core trailing updates are used by the mixed panel path when a size
-// class in range runs one team per CTA (the team then owns all of the SM's
-// TMEM) and, with the BF16 staging buffer, every class still fits the
-// shared-memory budget with one CTA per SM. KGB_NO_TC=1 in the environment
-// turns them off (FP32 FMA updates), for comparisons.
+// Tensor-core trailing updates are used by the mixed panel path when the
+// launch holds orders above PC_TC_NMIN, a size class in range runs one team
+// per CTA (the team then owns all of the SM's TMEM) and, with the BF16
+// staging buffer, every class still fits the shared-memory budget with one
+// CTA per SM; the launch then runs the kernel instantiation that carries the
+// tensor-core code. KGB_NO_TC=1 in the environment turns them off (FP32 FMA
+// updates), for comparisons.
 static inline bool tc_disabled_by_env() {
   const char *e = getenv("KGB_NO_TC");
   return e && e[0] == '1';
@@ -116,7 +118,7 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
     return true;
   };
   bool want_tc = false;
-  if (MIXED && (PATHS & 2) && !tc_disabled_by_env()) {
+  if (MIXED && (PATHS & 2) && max_n > PC_TC_NMIN && !tc_disabled_by_env()) {
     for (int c = 0; c < PC_NCLS; c++) {
       const int nlo = c ? pl.cfg.nmax[c - 1] + 1 : 1;
       const int nhi = pl.cfg.nmax[c] < max_n ? pl.cfg.nmax[c] : max_n;
@@ -128,23 +130,37 @@ static inline int plan_posv(KBlasHandle *h, int max_n, PosvPlan &pl) {
   if (!want_tc && !need(false, smem)) return KBLAS_NotSupported;
   if (smem == 0) smem = 16;
   pl.smem = (int)smem;
-  auto kern = posv_persistent_kernel<MIXED, PATHS>;
-  int st = set_smem(kern, smem);
-  if (st != KBLAS_Success) return st;
+  // the kernel instantiation launched: with the tensor-core code (PATHS bit
+  // 2) only when the plan uses it
+  auto occupancy = [&](bool tc, int bytes, int &per_sm) -> int {
+    int st = KBLAS_Success;
+    cudaError_t e = cudaSuccess;
+    per_sm = 0;
+    if constexpr (MIXED && (PATHS & 2) != 0) {
+      if (tc) {
+        auto kern = posv_persistent_kernel<MIXED, PATHS | 4>;
+        st = set_smem(kern, bytes);
+        if (st == KBLAS_Success) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, bytes);
+      }
+    }
+    if (!tc) {
+      auto kern = posv_persistent_kernel<MIXED, PATHS>;
+      st = set_smem(kern, bytes);
+      if (st == KBLAS_Success) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, bytes);
+    }
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    return st;
+  };
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  int st = occupancy(want_tc, pl.smem, per_sm);
+  if (st != KBLAS_Success) return st;
   // a CTA with tensor-core updates takes every TMEM column of its SM
   if (want_tc && per_sm > 1) {
     if (!need(false, smem)) return KBLAS_NotSupported;
     want_tc = false;
     pl.smem = (int)(smem ? smem : 16);
-    st = set_smem(kern, pl.smem);
+    st = occupancy(false, pl.smem, per_sm);
     if (st != KBLAS_Success) return st;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PC_NT, pl.smem) != cudaSuccess ||
-        per_sm < 1)
-      per_sm = 1;
   }
   pl.tc = want_tc ? 1 : 0;
   pl.grid = h->sm_count * per_sm;

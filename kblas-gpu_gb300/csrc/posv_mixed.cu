@@ -61,7 +61,9 @@ static int mixed_uniform(KBlasHandle *h, char side, char uplo, int m, int n, Sys
   OutArgs out{info, iter, base + ws.scratch, (long long)pl.slot_bytes, pl.tc, h->d_status};
   sys.n = n;
   sys.m = m;
-  if (n > 32)
+  if (n > 32 && pl.tc)
+    posv_persistent_kernel<true, 6><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+  else if (n > 32)
     posv_persistent_kernel<true, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
   else
     posv_persistent_kernel<true, 1><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
@@ -130,7 +132,9 @@ int mixed_uniform_fixed_scratch(cudaStream_t stream, int device, int sm_count, i
   it.queue = header;
   OutArgs out{info, iter, pl.slot_bytes ? scratch + head : nullptr, (long long)pl.slot_bytes,
               pl.tc, nullptr};
-  if (n > 32)
+  if (n > 32 && pl.tc)
+    posv_persistent_kernel<true, 6><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
+  else if (n > 32)
     posv_persistent_kernel<true, 2><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);
   else
     posv_persistent_kernel<true, 1><<<pl.grid, PC_NT, pl.smem, stream>>>(sys, it, out, pl.cfg, pl.smem);

@@ -214,7 +214,15 @@ static int vbatch(KBlasHandle *h, char side, char uplo, int *m, int *n, int max_
   // orders > 32 first (largest first), then orders <= 32 on the register path
   if (max_n > 32) {
     it.queue = header;
-    posv_persistent_kernel<MIXED, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+    bool launched = false;
+    if constexpr (MIXED) {
+      if (pl.tc) {
+        posv_persistent_kernel<MIXED, 6><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
+        launched = true;
+      }
+    }
+    if (!launched)
+      posv_persistent_kernel<MIXED, 2><<<pl.grid, PC_NT, pl.smem, h->stream>>>(sys, it, out, pl.cfg, pl.smem);
     KGB_LAUNCH_CHECK("posv_persistent_kernel");
   }
   it.queue = header + 2;

@@ -329,6 +329,40 @@ def test_vbatch_graph_capture_replay(gpu, handle, kb, wl, orc):
     assert (eta <= np.array([10 * n * EPS64 for n in ns])).all()
 
 
+@pytest.mark.parametrize("tc", [True, False], ids=["tensor_core", "ffma"])
+def test_vbatch_mixed_large_orders_tensor_core_kernel(gpu, handle, kb, wl, orc, monkeypatch, tc):
+    """A variable-size batch whose largest order exceeds 256 runs the kernel
+    with the tensor-core trailing update (orders 177.. on whole-CTA teams);
+    with KGB_NO_TC=1 the kernel without it. Both meet the bar on the same
+    batch, with 1..6 right-hand sides (residual sweeps over 1..4 at once)."""
+    if not tc:
+        monkeypatch.setenv("KGB_NO_TC", "1")
+    rng = np.random.default_rng(21)
+    batch = 40
+    ns = [int(x) for x in rng.integers(33, 400, batch)]
+    ns[0], ns[1], ns[2] = 400, 177, 257
+    ms = [int(x) for x in rng.integers(1, 7, batch)]
+    As, Bs = make_vbatch(wl, ns, ms, seed=500, indefinite={5})
+    Aout, Bout, info, it = run_vbatch(gpu, kb, handle, As, Bs, ns, ms, True)
+    refA = [a.copy() for a in As]
+    refB = [b.copy() for b in Bs]
+    ldas = [a.shape[1] for a in As]
+    ldbs = [b.shape[1] for b in Bs]
+    info_ref = orc.posv_vbatch(ms, ns, refA, ldas, refB, ldbs)
+    assert np.array_equal(info, info_ref)
+    assert info_ref[5] > 0
+    good = [i for i in range(batch) if info_ref[i] == 0]
+    eta = orc.backward_error_r_vbatch([ms[i] for i in good], [ns[i] for i in good],
+                                      [As[i] for i in good], [ldas[i] for i in good],
+                                      [Bout[i] for i in good], [ldbs[i] for i in good],
+                                      [Bs[i] for i in good], [ldbs[i] for i in good])
+    assert (eta <= np.array([10 * ns[i] * EPS64 for i in good])).all()
+    assert (it[good] >= 0).all()  # well-conditioned: refinement, no fallback
+    for i in good:
+        assert np.array_equal(Aout[i], As[i])
+    assert np.array_equal(Bout[5], Bs[5])
+
+
 def test_vbatch_needs_workspace(gpu, handle, kb):
     one = gpu.ones(4, dtype=gpu.int32, device="cuda")
     p = gpu.zeros(4, dtype=gpu.int64, device="cuda")
