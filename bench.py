@@ -1011,11 +1011,11 @@ def main():
     w.restore(full=True)
     # ---- end to end through the C ABI with pinned host buffers ----
     hA = torch.empty(w.pool_elems, dtype=torch.float64, pin_memory=True)
-    hA.copy_(w.A_pristine)
     hB = torch.empty(w.B0.numel(), dtype=torch.float64, pin_memory=True)
-    hB.copy_(w.B0)
     hX = torch.empty_like(hB, pin_memory=True)
-    hinfo = torch.empty(w.batch, dtype=torch.int32, pin_memory=True)
+    hinfo_all = torch.empty(w.batch, dtype=torch.int32, pin_memory=True)
+    hA.copy_(w.A_pristine)
+    hB.copy_(w.B0)
 
     # The batch is split into E2E_CHUNKS pieces that are contiguous in the
     # matrix pool (equal bytes); the host->device copy of piece k+1 runs on a
@@ -1038,45 +1038,69 @@ def main():
              "pA": w.pA[it_], "pB": w.pB[it_], "dn": w.dn[it_], "dm": w.dm[it_],
              "dldb": w.dldb[it_], "info": torch.zeros(len(idx), dtype=torch.int32, device="cuda"),
              "iter": torch.zeros(len(idx), dtype=torch.int32, device="cuda"),
-             "hinfo": torch.empty(len(idx), dtype=torch.int32, pin_memory=True),
+             "hinfo": hinfo_all[lo:hi],
              "ev": torch.cuda.Event()}
         kb.lib().kblas_posv_vbatch_wsquery(h.ptr, c["max_n"], c["n"])
         chunks.append(c)
     kb.check(h.allocate_workspace(), "kblasAllocateWorkspace")
     copy_stream = torch.cuda.Stream()
     ev_b = torch.cuda.Event()
-    # per-step duration of the host->device copies alone (copy stream), so a
-    # slow step can be told apart: slow copies vs slow solves
-    h2d_events = []
+    # per step: the duration of the host->device copies alone (copy stream) and
+    # the host time spent issuing the step, so that a slow step can be told
+    # apart -- slow copies, slow solves, or a host thread that stalled between
+    # two of the step's 35 calls while the GPU waited for the next one
+    h2d_events, host_ms = [], []
 
-    def e2e_step():
-        copy_stream.wait_stream(stream)
-        eh = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-        h2d_events.append(eh)
+    def e2e_body(s, timing):
+        copy_stream.wait_stream(s)
+        eh = None
+        if timing:
+            eh = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            h2d_events.append(eh)
         with torch.cuda.stream(copy_stream):
-            eh[0].record(copy_stream)
+            if eh:
+                eh[0].record(copy_stream)
             w.B.copy_(hB, non_blocking=True)
             ev_b.record(copy_stream)
             for c in chunks:
                 a_lo, a_hi = c["a"]
                 w.A[a_lo:a_hi].copy_(hA[a_lo:a_hi], non_blocking=True)
                 c["ev"].record(copy_stream)
-            eh[1].record(copy_stream)
-        stream.wait_event(ev_b)
+            if eh:
+                eh[1].record(copy_stream)
+        s.wait_event(ev_b)
         for c in chunks:
-            stream.wait_event(c["ev"])
+            s.wait_event(c["ev"])
             st = h.call("kblasDposv_vbatch_mixed", "R", "L", c["dm"].data_ptr(), c["dn"].data_ptr(),
                         1, c["max_n"], c["pA"].data_ptr(), c["dn"].data_ptr(), c["pB"].data_ptr(),
                         c["dldb"].data_ptr(), c["n"], c["info"].data_ptr(), c["iter"].data_ptr())
             if st != 1:
                 raise RuntimeError(f"kblasDposv_vbatch_mixed returned {st}")
-        hX.copy_(w.B, non_blocking=True)
-        for c in chunks:
-            c["hinfo"].copy_(c["info"], non_blocking=True)
+        with torch.cuda.stream(s):
+            hX.copy_(w.B, non_blocking=True)
+            for c in chunks:
+                c["hinfo"].copy_(c["info"], non_blocking=True)
 
-    t_e2e = timed_steps(torch, e2e_step, lambda: None, args.steps, args.warmup, stream)
+    def e2e_step():
+        t0 = time.perf_counter()
+        e2e_body(stream, True)
+        host_ms.append((time.perf_counter() - t0) * 1e3)
+
+    xm = x_mixed.numpy()
+
+    def e2e_results():
+        torch.cuda.synchronize()
+        e2e_info = np.zeros(w.batch, dtype=np.int32)
+        for c, (lo, hi) in zip(chunks, [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]):
+            e2e_info[order[lo:hi]] = c["hinfo"].numpy()
+        return {"info_equal": bool(np.array_equal(e2e_info, info)),
+                "max_rel_diff_x": float(np.abs(hX.numpy() - xm).max() / np.abs(xm).max())}
+
+    t_e2e_eager = timed_steps(torch, e2e_step, lambda: None, args.steps, args.warmup, stream)
     torch.cuda.synchronize()
     h2d_ms = [a.elapsed_time(b) for a, b in h2d_events[-args.steps:]]
+    host_issue_ms = host_ms[-args.steps:]
+    check_eager = e2e_results()
     # the host link alone: the same host->device copy of the matrix pool with
     # no solve running, repeated; its spread is the link's, not the solver's
     link_ms = []
@@ -1088,12 +1112,11 @@ def main():
             e1.record(copy_stream)
         e1.synchronize()
         link_ms.append(e0.elapsed_time(e1))
-    e2e_info = np.zeros(w.batch, dtype=np.int32)
-    for c, (lo, hi) in zip(chunks, [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]):
-        e2e_info[order[lo:hi]] = c["hinfo"].numpy()
-    xm = x_mixed.numpy()
-    e2e_check = {"info_equal": bool(np.array_equal(e2e_info, info)),
-                 "max_rel_diff_x": float(np.abs(hX.numpy() - xm).max() / np.abs(xm).max())}
+
+    def agrees(chk):
+        return chk is not None and chk["info_equal"] and chk["max_rel_diff_x"] <= 1e-10
+
+    t_e2e, e2e_check = t_e2e_eager, check_eager
     h2d = w.pool_elems * 8 + w.B0.numel() * 8
     d2h = w.B0.numel() * 8 + w.batch * 4
 
@@ -1108,7 +1131,7 @@ def main():
     v_fp64 = total_batch / (ms_fp64 * 1e-3)
     # an end-to-end run whose results differ from the resident run's (info
     # codes, or X beyond rounding of the summation order) has no rate
-    e2e_valid = e2e_check["info_equal"] and e2e_check["max_rel_diff_x"] <= 1e-10
+    e2e_valid = agrees(e2e_check)
     v_e2e = total_batch / (ms_e2e * 1e-3) if e2e_valid else None
     peaks = {}
     try:
@@ -1164,6 +1187,7 @@ def main():
                 "valid": e2e_valid,
                 "per_step_ms": [round(x, 3) for x in t_e2e],
                 "per_step_h2d_copy_ms": [round(x, 3) for x in h2d_ms],
+                "per_step_host_issue_ms": [round(x, 3) for x in host_issue_ms],
                 "host_link_probe_ms": [round(x, 3) for x in link_ms],
                 "host_link_probe": "the same host->device copy of the matrix pool (pinned, "
                                    "%.2f GB) with no solve running, %d times after the e2e steps"
