@@ -41,8 +41,13 @@ typedef struct KBlasHandle *kblasHandle_t;
  * Workspace queries (reference include/kblas_batch.h:485,773,786,1100,1113,
  * 1380,1391,2077,2089,2772,2785). Each call raises the handle's requested
  * workspace to what the routine needs; kblasAllocateWorkspace then allocates.
- * The uniform routines of this library need no workspace, so these only
- * record zero-byte requests; they are kept so KBLAS callers link unchanged.
+ * SYRK, TRSM and TRMM need none (zero-byte requests, kept so KBLAS callers
+ * link unchanged). The double-precision POTRF / POTRS / POSV of order 33..1024
+ * request scratch for the persistent panel kernel and run on it once the
+ * workspace is allocated; without it they run on a one-launch blocked kernel
+ * that needs none but is several times slower at small orders (about 14% of
+ * the FP64 peak at n = 64 against 33% with the workspace). Call the query and
+ * kblasAllocateWorkspace, as KBLAS callers do, before timing these routines.
  * ------------------------------------------------------------------------- */
 void kblas_syrk_batch_wsquery(kblasHandle_t handle, const int m, int batchCount);
 void kblas_trsm_batch_wsquery(kblasHandle_t handle, char side, int m, int n, int batchCount);
